@@ -1,0 +1,93 @@
+/*
+ * mpf3d.h -- C ABI of libmpf3d.so, the GB300 (sm_103a) implementation of the
+ * 3D multi-phase-field step of daikihatanaka0327/multiphasefield-solidification-v2.
+ *
+ * Plain pointers, sizes and a stream handle; no C++ or framework types.  All
+ * array pointers are DEVICE pointers unless a parameter says "host".  Every
+ * function enqueues asynchronously on `stream` (a cudaStream_t passed as
+ * void*, NULL = legacy default stream) and returns an MPF3D_* status code
+ * describing argument validation and the launch; conditions found on the
+ * device are OR-ed into the caller's optional `err` word (int32, device).
+ *
+ * Arrays use the reference's dense C-order layout:
+ *   phi  [N][nx][ny][nz]   float32 or float64   (z fastest)
+ *   mf   [depth][nx][ny][nz] int32,  nf [nx][ny][nz] int32
+ *   temp [nx][ny][nz]      float32 or float64
+ *   wij, aij, mij [N][N] float32,  n111 [N][8][3] float32
+ */
+#ifndef MPF3D_H
+#define MPF3D_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* return codes */
+#define MPF3D_OK 0
+#define MPF3D_ERR_ARG (-1)    /* bad size, null pointer or unsupported combination */
+#define MPF3D_ERR_DTYPE (-2)  /* dtype code not 0 (float32) or 1 (float64) */
+#define MPF3D_ERR_CUDA (-3)   /* a CUDA call or launch failed */
+#define MPF3D_ERR_TOO_LARGE (-4)
+
+/* dtype codes */
+#define MPF3D_F32 0
+#define MPF3D_F64 1
+
+/* bits OR-ed into the device `err` word */
+#define MPF3D_DEV_MF_DEPTH 1      /* unchecked APT needed more rows than mf has */
+#define MPF3D_DEV_NF_GT_KMAX 2    /* update met nf > KMAX (cell left untouched) */
+#define MPF3D_DEV_BAD_ID 4        /* update met an mf id outside [0, N) */
+#define MPF3D_DEV_SLOT_OVERFLOW 8 /* compact stepper: more phases than slots */
+#define MPF3D_DEV_BAD_INPUT 16    /* compact conversion met a negative/NaN phi */
+
+/* compile-time bound on active phases per cell (reference KMAX) */
+#define MPF3D_KMAX 50
+
+/* The 13 floating-point kernel arguments of the reference's phase update, in
+ * the reference's argument order; bit i of f32mask says argument i was a
+ * float32 (np.float32) rather than a float64, which changes the arithmetic
+ * type of several expressions exactly as in the reference. */
+enum {
+    MPF3D_S_DX = 0, MPF3D_S_DT, MPF3D_S_T_MELT, MPF3D_S_SF, MPF3D_S_EPS0_SL, MPF3D_S_W0_SL,
+    MPF3D_S_A0, MPF3D_S_DELTA_A, MPF3D_S_MU_A, MPF3D_S_P_ROUND, MPF3D_S_G2_FLOOR, MPF3D_S_KSI,
+    MPF3D_S_THETA_C_RAD, MPF3D_S_COUNT
+};
+typedef struct mpf3d_scalars {
+    double v[MPF3D_S_COUNT];
+    uint32_t f32mask;
+} mpf3d_scalars;
+
+/* ---- dense drop-in tier (reference numerics) ---------------------------- */
+
+/* Replaces kernel_update_nfmf_3d (checked = 0) and
+ * kernel_update_nfmf_3d_checked (checked = 1), src/gpu_kernels_3d.py:462-527.
+ * status: int32[2] device array, required when checked ({overflow, max n},
+ * atomic max as in the reference).  Unchecked writes are clamped to `depth`
+ * rows and set MPF3D_DEV_MF_DEPTH instead of running past the array. */
+int mpf3d_dense_apt(const void *phi, int phi_dtype, int N, int nx, int ny, int nz, int32_t *mf,
+                    int depth, int32_t *nf, int32_t *status, int checked, int32_t *err,
+                    void *stream);
+
+/* Replaces kernel_update_phasefield_active_3d (switchable = 0) and
+ * kernel_update_phasefield_active_3d_switchable (switchable = 1),
+ * src/gpu_kernels_3d.py:530-830.  phi and phi_new share phi_dtype. */
+int mpf3d_dense_update(const void *phi, void *phi_new, int phi_dtype, const void *temp,
+                       int temp_dtype, const int32_t *mf, int depth, const int32_t *nf,
+                       const float *wij, const float *aij, const float *mij, const float *n111,
+                       int N, int nx, int ny, int nz, const mpf3d_scalars *scalars, int switchable,
+                       int enable_anisotropy, int enable_torque, int32_t *err, void *stream);
+
+/* Replaces kernel_update_temp_3d, src/gpu_kernels_3d.py:833-838:
+ * temp -= cooling_rate (float32 arithmetic when both are float32). */
+int mpf3d_dense_temp(void *temp, int temp_dtype, double cooling_rate, int rate_is_f32, int64_t n,
+                     void *stream);
+
+/* library version, for the binding's load check */
+int mpf3d_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MPF3D_H */

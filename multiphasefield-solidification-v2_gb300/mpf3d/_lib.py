@@ -1,0 +1,77 @@
+"""ctypes binding of libmpf3d.so (the C ABI declared in include/mpf3d.h).
+
+There is no fallback: if the library is missing or fails to load, every
+entry point raises.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import os
+
+LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libmpf3d.so")
+
+MPF3D_OK = 0
+ERRORS = {-1: "bad argument", -2: "bad dtype", -3: "CUDA launch/call failed", -4: "size above limit"}
+
+DEV_BITS = {1: "unchecked APT needed more rows than mf has (MPF3D_DEV_MF_DEPTH)",
+            2: "update met nf > KMAX (MPF3D_DEV_NF_GT_KMAX)",
+            4: "update met an mf id outside [0, N) (MPF3D_DEV_BAD_ID)",
+            8: "compact stepper: more phases than slots (MPF3D_DEV_SLOT_OVERFLOW)",
+            16: "compact conversion met a negative or NaN phi (MPF3D_DEV_BAD_INPUT)"}
+
+_VP = ctypes.c_void_p
+_I32 = ctypes.c_int
+_I64 = ctypes.c_int64
+_F64 = ctypes.c_double
+
+
+class Scalars(ctypes.Structure):
+    """mpf3d_scalars: the 13 float arguments + float32 mask."""
+    _fields_ = [("v", ctypes.c_double * 13), ("f32mask", ctypes.c_uint32)]
+
+
+# name -> (restype, argtypes)
+_SIGS = {
+    "mpf3d_version": (_I32, []),
+    "mpf3d_dense_apt": (_I32, [_VP, _I32, _I32, _I32, _I32, _I32, _VP, _I32, _VP, _VP, _I32, _VP, _VP]),
+    "mpf3d_dense_update": (_I32, [_VP, _VP, _I32, _VP, _I32, _VP, _I32, _VP, _VP, _VP, _VP, _VP,
+                                  _I32, _I32, _I32, _I32, ctypes.POINTER(Scalars), _I32, _I32, _I32,
+                                  _VP, _VP]),
+    "mpf3d_dense_temp": (_I32, [_VP, _I32, _F64, _I32, _I64, _VP]),
+}
+
+_LIB = None
+
+
+class LibraryMissing(RuntimeError):
+    pass
+
+
+def lib():
+    global _LIB
+    if _LIB is None:
+        if not os.path.exists(LIB_PATH):
+            raise LibraryMissing(f"{LIB_PATH} is not built: run `python -c \"import __graft_entry__ as g; "
+                                 "g.build()\"` (or multiphasefield-solidification-v2_gb300/build.py)")
+        L = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in _SIGS.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _LIB = L
+    return _LIB
+
+
+def exported_symbols():
+    """Names the binding expects the library to export."""
+    return list(_SIGS)
+
+
+def check(rc: int, what: str) -> None:
+    if rc != MPF3D_OK:
+        raise RuntimeError(f"{what} failed: {ERRORS.get(rc, rc)}")
+
+
+def describe_dev_error(word: int) -> str:
+    return "; ".join(msg for bit, msg in DEV_BITS.items() if word & bit) or "none"
