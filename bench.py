@@ -1,0 +1,383 @@
+"""Benchmark of the 3D multi-phase-field step on GB300.
+
+Workload (default): 256^3 grid, 64 grains seeded uniformly in the bottom 32
+z-layers (3D Voronoi) plus liquid (N = 65 phases), tanh front, anisotropy and
+torque on, uniform cooling, config_3d.yaml physics, 2000 steps -- advanced by
+the compact FP32 fused stepper (one kernel per step).  Synthetic seeded
+inputs of the configured shape; no dataset is involved.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line (rank 0).  `value` is cell-steps/s with the state
+resident in HBM; `e2e` runs the same job through the public API from pinned
+host memory (dense phi in, dense phi out) with the copies timed.  The
+reference arm (--impl reference) times the CPU oracle -- a C restatement of
+the reference kernels with their float32 typing -- on all host cores over a
+bounded crop of the same workload.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "multiphasefield-solidification-v2_gb300")
+for p in (PKG, ROOT):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+METRIC = "3D cell-steps/s (FP32 compact step, 256^3, N=65)"
+UNIT = "cell-steps/s"
+GRID = (256, 256, 256)
+N_GRAINS = 64
+SLAB = 32
+SEED, ORIENT_SEED = 2026, 7
+FALLBACK_HBM_GBS = 6800.0
+
+
+def workload_owner(nx, ny, nz):
+    from mpf3d import inputs
+    return inputs.voronoi_slab_owner(nx, ny, nz, N_GRAINS, SLAB, SEED)
+
+
+def workload_inputs(phys):
+    from mpf3d import inputs
+    q = inputs.random_quaternions(N_GRAINS, ORIENT_SEED)
+    wij, aij, mij = inputs.matrices_for(phys, N_GRAINS + 1)
+    return inputs.rotated_n111(q), wij, aij, mij
+
+
+def dense_phi_on_device(owner_t, prof_t, torch):
+    """Dense phi [N, nx, ny, nz] built on the GPU from the owner map."""
+    nx, ny, nz = owner_t.shape
+    phi = torch.zeros((N_GRAINS + 1, nx, ny, nz), dtype=torch.float32, device=owner_t.device)
+    solid = prof_t.view(1, 1, nz).expand(nx, ny, nz)
+    phi.scatter_(0, owner_t.long().unsqueeze(0), solid.unsqueeze(0).contiguous())
+    phi[0] = torch.clamp(1.0 - phi[1:].sum(dim=0), 0.0, 1.0)
+    return phi
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+            time.sleep(0.3)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            time.sleep(0.15)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.path or not os.path.exists(self.path):
+            return None
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[3:7]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+def measured_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def committed_traffic():
+    """Per-launch DRAM bytes of the step kernel from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "compact_step_256cube.txt")
+    try:
+        for line in open(path):
+            if line.startswith("dram_bytes_per_launch_full_size:"):
+                return float(line.split(":", 1)[1].split()[0])
+    except OSError:
+        pass
+    return None
+
+
+def cpu_oracle_rate(phys, cx, cy, seconds, max_steps=None, warmup=0):
+    """Oracle (reference typing: float32 phi and scalars) on a cx x cy x 256
+    crop of the workload; returns (cell-steps/s, steps, cells, threads)."""
+    import oracle as O
+    from mpf3d import inputs
+    nz = GRID[2]
+    owner = workload_owner(GRID[0], GRID[1], nz)[:cx, :cy, :].copy()
+    d = phys.derived()
+    prof = inputs.tanh_profile(nz, SLAB, phys.dx, d["delta"])
+    phi = inputs.phi_from_owner(owner, N_GRAINS, prof)
+    temp = inputs.temperature_field(cx, cy, nz, phys.T_melt, phys.G, phys.dx, SLAB)
+    n111, wij, aij, mij = workload_inputs(phys)
+    sc = O.make_scalars([float(v) for v in phys.kernel_scalars(True)], True)
+    rate = d["cooling_rate"]
+    phi_new = phi.copy()
+    mf = np.zeros((50, cx, cy, nz), np.int32)
+    nf = np.zeros((cx, cy, nz), np.int32)
+
+    def one():
+        nonlocal phi, phi_new
+        O.temp_step(temp, rate, True)
+        st = np.zeros(2, np.int32)
+        O.apt(phi, mf, nf, st, checked=True)
+        O.update(phi, phi_new, temp, mf, nf, wij, aij, mij, n111, sc, switchable=False)
+        phi, phi_new = phi_new, phi
+
+    for _ in range(warmup):
+        one()
+    t0 = time.perf_counter()
+    steps = 0
+    while True:
+        one()
+        steps += 1
+        el = time.perf_counter() - t0
+        if (max_steps is not None and steps >= max_steps) or (max_steps is None and el >= seconds):
+            break
+    cells = cx * cy * nz
+    threads = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    return cells * steps / el, steps, cells, threads
+
+
+def run_reference(args, rank):
+    if rank != 0:
+        return
+    from mpf3d.inputs import Physics
+    phys = Physics()
+    total = args.steps + args.warmup
+    # crop sized so that the whole run stays within about two minutes
+    side = 64 if total <= 60 else (32 if total <= 400 else 16)
+    val, steps, cells, threads = cpu_oracle_rate(phys, side, side, 0.0, max_steps=args.steps,
+                                                 warmup=args.warmup)
+    sample = f"{side}x{side}x256 crop of the workload (N=65), {steps} oracle steps"
+    line = {"impl": "reference", "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 storage, f64/f32 reference typing",
+            "data": "synthetic", "config": config_dict(args),
+            "cpu_baseline": {"value": val, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def config_dict(args):
+    return {"workload": "3D random Voronoi 256^3, 64 grains in the bottom 32 z-layers + liquid "
+                        "(N=65), tanh front, anisotropy+torque on, uniform cooling (config_3d.yaml), "
+                        "FP32 compact fused step",
+            "grid": list(GRID), "phases": N_GRAINS + 1, "slots": args.slots, "steps": args.steps,
+            "l2": "inputs larger than L2 (compact state > 129 MB per step)",
+            "parallelism": f"replicas x{args.gpus}" if args.gpus > 1 else "single GPU"}
+
+
+def run_ours(args, rank, world):
+    import torch
+    from mpf3d import inputs
+    from mpf3d.solver import CompactSolver
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dev = torch.device(f"cuda:{local}")
+    torch.cuda.set_device(dev)
+    phys = inputs.Physics()
+    d = phys.derived()
+    nx, ny, nz = GRID
+    owner = torch.from_numpy(workload_owner(nx, ny, nz)).to(dev)
+    prof = torch.from_numpy(inputs.tanh_profile(nz, SLAB, phys.dx, d["delta"])).to(dev)
+    temp = inputs.temperature_field(1, 1, nz, phys.T_melt, phys.G, phys.dx, SLAB)[0, 0]
+    n111, wij, aij, mij = workload_inputs(phys)
+    phi0 = dense_phi_on_device(owner, prof, torch)
+    solver = CompactSolver(phi0, temp, n111, wij, aij, mij, phys, slots=args.slots)
+    stream = torch.cuda.current_stream(dev)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    # warm-up, then restart the job from the initial state
+    solver.step(args.warmup)
+    torch.cuda.synchronize(dev)
+    solver = CompactSolver(phi0, temp, n111, wij, aij, mij, phys, slots=args.slots)
+    torch.cuda.synchronize(dev)
+
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        barrier()
+        torch.cuda.synchronize(dev)
+        e0.record(stream)
+        for i in range(args.steps):
+            solver.launch_step(i + 1)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        barrier()
+    solver.check()
+    ms = e0.elapsed_time(e1)
+    if world > 1:
+        t = torch.tensor([ms], dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    final_cnt_sum = int(solver.stored_counts().sum(dtype=torch.int64).item())
+
+    # accounting pass (untimed): stored-slot occupancy of every step
+    acc = CompactSolver(phi0, temp, n111, wij, aij, mij, phys, slots=args.slots)
+    occ = [int(acc.stored_counts().sum(dtype=torch.int64).item())]
+    for i in range(args.steps):
+        acc.launch_step(i + 1)
+        occ.append(int(acc.stored_counts().sum(dtype=torch.int64).item()))
+    acc.check()
+    del acc
+    cells = nx * ny * nz
+    # algorithmic bytes: read and write every cell's record once (1-byte count
+    # plus 6 bytes per stored phase)
+    bytes_total = sum(2 * cells + 6 * (occ[i] + occ[i + 1]) for i in range(args.steps))
+    bytes_per_launch = bytes_total / args.steps
+    sec = ms / 1e3
+    value = cells * args.steps * world / sec
+    per_launch_s = sec / args.steps
+    peak, peak_kind = measured_peak()
+    achieved = bytes_per_launch / per_launch_s / 1e9
+    traffic = committed_traffic()
+
+    # end to end through the public API: pinned dense phi in, dense phi out
+    if args.no_e2e:
+        t_e2e, in_bytes, out_bytes = float("nan"), 0, 0
+    else:
+        t_e2e, in_bytes, out_bytes = e2e_run(args, phi0, temp, n111, wij, aij, mij, phys, dev, barrier, world)
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        v, st, cl, th = cpu_oracle_rate(phys, 64, 64, 10.0)
+        cpu = {"value": v, "unit": UNIT, "cores": th, "kind": "port",
+               "sample": f"64x64x256 crop of the workload (N=65), {st} oracle steps (reference "
+                         f"float32 typing), OpenMP"}
+    emit(args, rank, world, ms, cells, t_e2e, in_bytes, out_bytes, achieved, peak, peak_kind,
+         traffic, bytes_per_launch, occ, clk, cpu, final_cnt_sum)
+
+
+def e2e_run(args, phi0, temp, n111, wij, aij, mij, phys, dev, barrier, world):
+    import torch
+    from mpf3d.solver import CompactSolver
+    phi_host = phi0.cpu().pin_memory()
+    out_host = torch.empty_like(phi_host).pin_memory()
+    torch.cuda.synchronize(dev)
+    barrier()
+    t0 = time.perf_counter()
+    dphi = phi_host.to(dev, non_blocking=True)
+    s2 = CompactSolver(dphi, temp, n111, wij, aij, mij, phys, slots=args.slots)
+    s2.step(args.steps, check=False)
+    out_host.copy_(s2.to_dense(host=False), non_blocking=True)
+    torch.cuda.synchronize(dev)
+    t_e2e = time.perf_counter() - t0
+    s2.check()
+    barrier()
+    if world > 1:
+        t = torch.tensor([t_e2e], dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        t_e2e = float(t.item())
+    in_bytes = phi_host.numel() * 4 + temp.nbytes + n111.nbytes + 3 * wij.nbytes
+    out_bytes = out_host.numel() * 4
+    return t_e2e, in_bytes, out_bytes
+
+
+def emit(args, rank, world, ms, cells, t_e2e, in_bytes, out_bytes, achieved, peak, peak_kind,
+         traffic, bytes_per_launch, occ, clk, cpu, final_cnt_sum):
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": config_dict(args),
+                "e2e": {"value": cells * args.steps * world / t_e2e, "unit": UNIT,
+                        "h2d_bytes_per_step": in_bytes / args.steps,
+                        "d2h_bytes_per_step": out_bytes / args.steps},
+                "gpu_launches": args.steps,
+                "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                             "frac": achieved / peak, "traffic": traffic,
+                             "peak_source": peak_kind,
+                             "bytes_per_cell_step": bytes_per_launch / cells,
+                             "kernel": "mpf3d::compact::step_kernel<8,16>"},
+                "stored_phases_per_cell": {"start": occ[0] / cells, "end": occ[-1] / cells},
+                "clocks": clk.summary(),
+                "cpu_baseline": cpu}
+        assert final_cnt_sum == occ[-1], "timed and accounting runs diverged"
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--slots", type=int, default=8)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end run (profiling)")
+    ap.add_argument("--grid", type=int, nargs=3, default=None,
+                    help="override the 256^3 grid (smaller cases for profiling)")
+    args = ap.parse_args()
+    global GRID
+    if args.grid:
+        GRID = tuple(args.grid)
+    if args.warmup < 3:
+        args.warmup = 3
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if world > 1 and args.impl == "ours":
+        import torch
+        torch.distributed.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    if args.impl == "reference":
+        run_reference(args, rank)
+    else:
+        run_ours(args, rank, world)
+    if world > 1 and args.impl == "ours":
+        import torch
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

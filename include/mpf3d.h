@@ -84,6 +84,40 @@ int mpf3d_dense_update(const void *phi, void *phi_new, int phi_dtype, const void
 int mpf3d_dense_temp(void *temp, int temp_dtype, double cooling_rate, int rate_is_f32, int64_t n,
                      void *stream);
 
+/* ---- compact FP32 tier (fused step) -------------------------------------
+ * State of one buffer (x fastest: cell = (k*ny + m)*nx + l):
+ *   cnt uint8[cells], idx uint16[slots][cells] (ascending ids), val float[slots][cells]
+ * slots is 4, 8 or 16.  No reference counterpart for the layout: it replaces
+ * the dense phi [N][nx][ny][nz] + mf/nf arrays of src/gpu_kernels_3d.py. */
+
+/* dense phi (z fastest, float32/float64) -> compact state.  Negative or NaN
+ * entries set MPF3D_DEV_BAD_INPUT; more than `slots` positive phases in a
+ * cell set MPF3D_DEV_SLOT_OVERFLOW. */
+int mpf3d_compact_from_dense(const void *phi, int phi_dtype, int N, int nx, int ny, int nz, int slots,
+                             uint8_t *cnt, uint16_t *idx, float *val, int32_t *err, void *stream);
+
+/* compact state -> dense phi (every phase written, zeros included). */
+int mpf3d_compact_to_dense(const uint8_t *cnt, const uint16_t *idx, const float *val, int slots, int N,
+                           int nx, int ny, int nz, void *phi, int phi_dtype, void *stream);
+
+/* nf of the reference's APT (kernel_update_nfmf_3d, src/gpu_kernels_3d.py:462-486)
+ * computed from a compact state, dense z-fastest int32 output. */
+int mpf3d_compact_active_count(const uint8_t *cnt, const uint16_t *idx, int slots, int nx, int ny, int nz,
+                               int32_t *nf, void *stream);
+
+/* One fused time step in FP32: APT rebuild (src/gpu_kernels_3d.py:462-486),
+ * phase update of kernel_update_phasefield_active_3d_switchable (:683-830)
+ * and the cooling of kernel_update_temp_3d (:833-838) folded into
+ * T = T0z[k] - (Tm_plus_cool - T_melt).  (slots, amax) is (4, 8), (8, 16) or
+ * (16, 32); more active phases than amax, or more positive phases than
+ * slots, leave the cell unchanged and set MPF3D_DEV_SLOT_OVERFLOW.
+ * a2ij = aij*aij elementwise (float32).  T0z: float64 [nz]. */
+int mpf3d_compact_step(const uint8_t *cnt, const uint16_t *idx, const float *val, uint8_t *cnt_out,
+                       uint16_t *idx_out, float *val_out, int slots, int amax, const double *T0z,
+                       double Tm_plus_cool, const float *wij, const float *a2ij, const float *mij,
+                       const float *n111, int N, int nx, int ny, int nz, const mpf3d_scalars *scalars,
+                       int enable_anisotropy, int enable_torque, int32_t *err, void *stream);
+
 /* library version, for the binding's load check */
 int mpf3d_version(void);
 

@@ -1,0 +1,643 @@
+// compact.cu -- fused FP32 compact-slot stepper (throughput tier).
+//
+// One kernel per time step does what the reference does in three launches
+// (src/gpu_kernels_3d.py:462-486 APT rebuild, :530-680 phase update,
+// :833-838 cooling): it rebuilds each cell's active-phase list from the
+// stored lists of the cell and its 6 face neighbours, evaluates the
+// anisotropic interface, torque and kinetic terms and the pair sums, clips,
+// renormalises and writes only the phases that stay positive.
+//
+// State layout in HBM (x fastest, so a warp of 32 threads along x reads
+// 32 consecutive entries of each array and an interface -- normal to z --
+// keeps a warp convergent):
+//   cnt  uint8 [cells]            number of stored phases (phi > 0)
+//   idx  uint16[S][cells]         stored phase ids, ascending
+//   val  float [S][cells]         stored phase fractions
+// Temperature is T0[z] - (accumulated cooling) with the accumulator in
+// float64 on the host; the per-cell sum-to-one uses a compensated float
+// pair (TwoSum), which keeps GB300's slow float64 pipe out of the loop.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#include "mpf3d.h"
+#include "mpf3d_internal.h"
+
+namespace mpf3d {
+namespace compact {
+
+constexpr int LIQ = 0;
+// the reference's pi approximation in the driving-force prefactor (:651)
+constexpr float FORCE_PREF = (float)(8.0 / 3.1415926535);
+
+struct Params {
+    int nx, ny, nz, N;
+    int64_t cells;
+    float inv_dx2, inv_2dx, half_over_dx, inv_dx, dt;
+    float eps0, eps0sq, w0, mu_a, delta_a, mu_da, pp, tan_a0, g2_floor, ksi, theta_c, Sf;
+    double Tmc;  // T_melt + accumulated cooling (float64)
+    int use_aniso, use_torque;
+};
+
+struct In {
+    const uint8_t *__restrict__ cnt;
+    const uint16_t *__restrict__ idx;
+    const float *__restrict__ val;
+};
+struct Out {
+    uint8_t *__restrict__ cnt;
+    uint16_t *__restrict__ idx;
+    float *__restrict__ val;
+};
+
+__device__ __forceinline__ int wrap_p(int l, int n) { return l < n - 1 ? l + 1 : 0; }
+__device__ __forceinline__ int wrap_m(int l, int n) { return l > 0 ? l - 1 : n - 1; }
+__device__ __forceinline__ int clamp_p(int k, int n) { return k < n - 1 ? k + 1 : n - 1; }
+__device__ __forceinline__ int clamp_m(int k, int n) { return k > 0 ? k - 1 : 0; }
+
+__device__ __forceinline__ int64_t cell_of(const Params &P, int l, int m, int k) {
+    return ((int64_t)k * P.ny + m) * P.nx + l;
+}
+
+// stored fraction of phase `id` at cell q (0 when not stored)
+template <int S>
+__device__ __forceinline__ float lookup(const In &in, int64_t cells, int64_t q, int id) {
+    int c = __ldg(in.cnt + q);
+    c = c < S ? c : S;
+    for (int s = 0; s < c; ++s) {
+        int v = __ldg(in.idx + s * cells + q);
+        if (v == id) return __ldg(in.val + s * cells + q);
+        if (v > id) break;
+    }
+    return 0.0f;
+}
+
+// liquid fraction at cell q: the liquid (id 0) sorts first when stored
+__device__ __forceinline__ float liquid_at(const In &in, int64_t cells, int64_t q) {
+    int c = __ldg(in.cnt + q);
+    if (c == 0 || __ldg(in.idx + q) != LIQ) return 0.0f;
+    return __ldg(in.val + q);
+}
+
+__device__ __forceinline__ float3 grad_liquid(const In &in, const Params &P, int l, int m, int k) {
+    int lp = wrap_p(l, P.nx), lm = wrap_m(l, P.nx), mp = wrap_p(m, P.ny), mm = wrap_m(m, P.ny);
+    int kp = clamp_p(k, P.nz), km = clamp_m(k, P.nz);
+    float3 g;
+    g.x = (liquid_at(in, P.cells, cell_of(P, lp, m, k)) - liquid_at(in, P.cells, cell_of(P, lm, m, k))) * P.inv_2dx;
+    g.y = (liquid_at(in, P.cells, cell_of(P, l, mp, k)) - liquid_at(in, P.cells, cell_of(P, l, mm, k))) * P.inv_2dx;
+    g.z = (liquid_at(in, P.cells, cell_of(P, l, m, kp)) - liquid_at(in, P.cells, cell_of(P, l, m, km))) * P.inv_2dx;
+    return g;
+}
+
+// max |cos| between a gradient and the grain's 8 rotated {111} normals, with
+// the signed cosine and the winning normal (best_cos_from_grad_3d :110-134,
+// facet_cos_and_nxyz_from_grad :251-301)
+struct Facet {
+    bool valid;
+    float cabs, cs, nx, ny, nz, q;
+};
+
+__device__ __forceinline__ Facet facet(float3 g, const float *__restrict__ u, float g2_floor) {
+    Facet f;
+    f.q = g.x * g.x + g.y * g.y + g.z * g.z;
+    f.valid = !(f.q < g2_floor);
+    f.cabs = 0.0f; f.cs = 0.0f; f.nx = 1.0f; f.ny = 0.0f; f.nz = 0.0f;
+    if (!f.valid) return f;
+    float ig = rsqrtf(f.q);
+    float gx = g.x * ig, gy = g.y * ig, gz = g.z * ig;
+#pragma unroll
+    for (int t = 0; t < 8; ++t) {
+        float ux = __ldg(u + 3 * t), uy = __ldg(u + 3 * t + 1), uz = __ldg(u + 3 * t + 2);
+        float d = gx * ux + gy * uy + gz * uz;
+        float a = fabsf(d);
+        if (a > f.cabs) {
+            f.cabs = a; f.cs = d; f.nx = ux; f.ny = uy; f.nz = uz;
+        }
+    }
+    f.cabs = fminf(f.cabs, 1.0f);
+    f.cs = fminf(fmaxf(f.cs, -1.0f), 1.0f);
+    return f;
+}
+
+// a(theta) (calc_a_from_cos :24-30)
+__device__ __forceinline__ float calc_a(const Params &P, float c) {
+    float c2 = c * c;
+    float C = sqrtf(c2 + P.pp);
+    float S = sqrtf(fmaxf(1.0f - c2, 0.0f) + P.pp);
+    return P.mu_a * (1.0f + P.delta_a * (C + P.tan_a0 * S));
+}
+
+// b(theta) (calc_b_from_cos :33-55)
+__device__ __forceinline__ float calc_b(const Params &P, float c) {
+    c = fminf(fmaxf(c, -1.0f), 1.0f);
+    float theta = acosf(c);
+    if (theta >= P.theta_c) return 1.0f;
+    const float hp = 1.57079632679489662f;
+    float y = hp * (theta / P.theta_c);
+    y = fminf(fmaxf(y, 1.0e-6f), hp - 1.0e-6f);
+    float t = tanf(y);
+    return P.ksi + (1.0f - P.ksi) * t * tanhf(1.0f / t);
+}
+
+// d a / d(grad phi) (da_dphixyz_A12 :304-341); returns a and the 3 components
+__device__ __forceinline__ float4 da_dgrad(const Params &P, float3 g, const Facet &f) {
+    if (!f.valid) return make_float4(0.f, 0.f, 0.f, 0.f);
+    float a = calc_a(P, f.cabs);
+    float ig = rsqrtf(f.q);
+    float ig3 = ig * ig * ig;
+    float ud = g.x * f.nx + g.y * f.ny + g.z * f.nz;
+    float c = f.cs, c2 = c * c;
+    float C = sqrtf(c2 + P.pp);
+    float S = sqrtf(fmaxf(1.0f - c2, 0.0f) + P.pp);
+    float coef = P.mu_da * (c / C - P.tan_a0 * (c / S));
+    return make_float4(a, coef * (f.nx * ig - ud * g.x * ig3), coef * (f.ny * ig - ud * g.y * ig3),
+                       coef * (f.nz * ig - ud * g.z * ig3));
+}
+
+template <int S, int AMAX>
+__global__ void __launch_bounds__(256) step_kernel(In in, Out out, const double *__restrict__ T0z,
+                                                   const float *__restrict__ wij, const float *__restrict__ a2ij,
+                                                   const float *__restrict__ mij, const float *__restrict__ n111,
+                                                   Params P, int32_t *__restrict__ err) {
+    const int l = blockIdx.x * blockDim.x + threadIdx.x;
+    const int m = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z * blockDim.z + threadIdx.z;
+    if (l >= P.nx || m >= P.ny || k >= P.nz) return;
+    const int64_t cells = P.cells;
+    const int lp = wrap_p(l, P.nx), lm = wrap_m(l, P.nx), mp = wrap_p(m, P.ny), mm = wrap_m(m, P.ny);
+    const int kp = clamp_p(k, P.nz), km = clamp_m(k, P.nz);
+    int64_t pt[7];
+    pt[0] = cell_of(P, l, m, k);
+    pt[1] = cell_of(P, lp, m, k);
+    pt[2] = cell_of(P, lm, m, k);
+    pt[3] = cell_of(P, l, mp, k);
+    pt[4] = cell_of(P, l, mm, k);
+    pt[5] = cell_of(P, l, m, kp);
+    pt[6] = cell_of(P, l, m, km);
+    const int64_t c = pt[0];
+
+    // fast path: the cell and its 6 neighbours hold one and the same phase.
+    // Then the active list is that phase alone, the pair sums are empty and
+    // the renormalised fraction is exactly 1.
+    const int c0 = __ldg(in.cnt + c);
+    const int i0 = __ldg(in.idx + c);
+    bool uniform = (c0 == 1);
+#pragma unroll
+    for (int p = 1; p < 7; ++p)
+        uniform = uniform && (__ldg(in.cnt + pt[p]) == 1) && (__ldg(in.idx + pt[p]) == i0);
+    if (uniform) {
+        out.cnt[c] = 1;
+        out.idx[c] = (uint16_t)i0;
+        out.val[c] = 1.0f;
+        return;
+    }
+
+    // active list: ascending union of the 7 stored lists (the APT rule of
+    // kernel_update_nfmf_3d for phi >= 0)
+    int ids[AMAX];
+    int n = 0;
+    bool ovf = false;
+    for (int p = 0; p < 7; ++p) {
+        const int64_t q = pt[p];
+        int cq = __ldg(in.cnt + q);
+        cq = cq < S ? cq : S;
+        for (int s = 0; s < cq; ++s) {
+            const int id = __ldg(in.idx + s * cells + q);
+            int pos = n;
+            bool dup = false;
+            for (int j = 0; j < n; ++j) {
+                if (ids[j] == id) { dup = true; break; }
+                if (ids[j] > id) { pos = j; break; }
+            }
+            if (dup) continue;
+            if (n == AMAX) { ovf = true; continue; }
+            for (int j = n; j > pos; --j) ids[j] = ids[j - 1];
+            ids[pos] = id;
+            ++n;
+        }
+    }
+    if (ovf) {
+        // leave the cell as it was and report; the host re-runs the step
+        // with a wider template
+        atomicOr(err, MPF3D_DEV_SLOT_OVERFLOW);
+        out.cnt[c] = (uint8_t)(c0 < S ? c0 : S);
+        for (int s = 0; s < c0 && s < S; ++s) {
+            out.idx[s * cells + c] = __ldg(in.idx + s * cells + c);
+            out.val[s * cells + c] = __ldg(in.val + s * cells + c);
+        }
+        return;
+    }
+
+    float vc[AMAX], lapk[AMAX];
+    for (int t = 0; t < n; ++t) {
+        const int id = ids[t];
+        const float v = lookup<S>(in, cells, c, id);
+        float s6 = lookup<S>(in, cells, pt[1], id) + lookup<S>(in, cells, pt[2], id);
+        s6 += lookup<S>(in, cells, pt[3], id);
+        s6 += lookup<S>(in, cells, pt[4], id);
+        s6 += lookup<S>(in, cells, pt[5], id);
+        s6 += lookup<S>(in, cells, pt[6], id);
+        vc[t] = v;
+        lapk[t] = (s6 - 6.0f * v) * P.inv_dx2;
+    }
+
+    const bool has_liq = n > 0 && ids[0] == LIQ;
+    const bool has_solid = n > (has_liq ? 1 : 0);
+    float lap_sl[AMAX], b_sl[AMAX];
+    float w_sl = P.w0;
+    for (int t = 0; t < n; ++t) {
+        lap_sl[t] = 0.0f;
+        b_sl[t] = 1.0f;
+    }
+    if (has_liq && has_solid) {
+        if (P.use_aniso) {
+            const int pl[7] = {l, lp, lm, l, l, l, l};
+            const int pm[7] = {m, m, m, mp, mm, m, m};
+            const int pk[7] = {k, k, k, k, k, kp, km};
+            float3 G[7];
+#pragma unroll
+            for (int p = 0; p < 7; ++p) G[p] = grad_liquid(in, P, pl[p], pm[p], pk[p]);
+            const float Lc = vc[0];
+            float Lp[7];
+#pragma unroll
+            for (int p = 1; p < 7; ++p) Lp[p] = liquid_at(in, cells, pt[p]);
+            // second derivatives of the liquid at the cell (d2_phi_xyz :207-248)
+            float pxx = 0.f, pyy = 0.f, pzz = 0.f, pxy = 0.f, pxz = 0.f, pyz = 0.f;
+            if (P.use_torque) {
+                pxx = (Lp[1] - 2.0f * Lc + Lp[2]) * P.inv_dx2;
+                pyy = (Lp[3] - 2.0f * Lc + Lp[4]) * P.inv_dx2;
+                pzz = (Lp[5] - 2.0f * Lc + Lp[6]) * P.inv_dx2;
+                const float qq = 0.25f * P.inv_dx2;
+                pxy = (liquid_at(in, cells, cell_of(P, lp, mp, k)) - liquid_at(in, cells, cell_of(P, lp, mm, k)) -
+                       liquid_at(in, cells, cell_of(P, lm, mp, k)) + liquid_at(in, cells, cell_of(P, lm, mm, k))) * qq;
+                pxz = (liquid_at(in, cells, cell_of(P, lp, m, kp)) - liquid_at(in, cells, cell_of(P, lp, m, km)) -
+                       liquid_at(in, cells, cell_of(P, lm, m, kp)) + liquid_at(in, cells, cell_of(P, lm, m, km))) * qq;
+                pyz = (liquid_at(in, cells, cell_of(P, l, mp, kp)) - liquid_at(in, cells, cell_of(P, l, mp, km)) -
+                       liquid_at(in, cells, cell_of(P, l, mm, kp)) + liquid_at(in, cells, cell_of(P, l, mm, km))) * qq;
+            }
+            for (int t = 1; t < n; ++t) {
+                const int g = ids[t];
+                const float *u = n111 + (size_t)g * 24;
+                Facet F[7];
+#pragma unroll
+                for (int p = 0; p < 7; ++p) F[p] = facet(G[p], u, P.g2_floor);
+                // div(eps^2 grad phi_L) with face-averaged eps^2 (aniso_term1_solid_3d :149-204)
+                float e2[7];
+#pragma unroll
+                for (int p = 0; p < 7; ++p) {
+                    const float e = P.eps0 * calc_a(P, F[p].cabs);
+                    e2[p] = e * e;
+                }
+                const float h = P.inv_2dx * P.inv_dx;
+                float lap_val = ((e2[0] + e2[1]) * (Lp[1] - Lc) - (e2[0] + e2[2]) * (Lc - Lp[2])) * h +
+                                ((e2[0] + e2[3]) * (Lp[3] - Lc) - (e2[0] + e2[4]) * (Lc - Lp[4])) * h +
+                                ((e2[0] + e2[5]) * (Lp[5] - Lc) - (e2[0] + e2[6]) * (Lc - Lp[6])) * h;
+                // torque (torque_A11_3d :386-441)
+                if (P.use_torque && F[0].valid) {
+                    const float3 g0 = G[0];
+                    const float q = F[0].q;
+                    const float qx = 2.0f * (g0.x * pxx + g0.y * pxy + g0.z * pxz);
+                    const float qy = 2.0f * (g0.x * pxy + g0.y * pyy + g0.z * pyz);
+                    const float qz = 2.0f * (g0.x * pxz + g0.y * pyz + g0.z * pzz);
+                    const float4 d0 = da_dgrad(P, g0, F[0]);
+                    const float ig = rsqrtf(q), ig3 = ig * ig * ig;
+                    const float ud = g0.x * F[0].nx + g0.y * F[0].ny + g0.z * F[0].nz;
+                    const float dcx = F[0].nx * ig - ud * g0.x * ig3;
+                    const float dcy = F[0].ny * ig - ud * g0.y * ig3;
+                    const float dcz = F[0].nz * ig - ud * g0.z * ig3;
+                    const float cxx = dcx * pxx + dcy * pxy + dcz * pxz;
+                    const float cyy = dcx * pxy + dcy * pyy + dcz * pyz;
+                    const float czz = dcx * pxz + dcy * pyz + dcz * pzz;
+                    const float cs = F[0].cs, cs2 = cs * cs;
+                    const float coef = P.mu_da * (cs / sqrtf(cs2 + P.pp) - P.tan_a0 * (cs / sqrtf(fmaxf(1.0f - cs2, 0.0f) + P.pp)));
+                    // A13_divergence_3d (:344-383)
+                    const float ddx = (da_dgrad(P, G[1], F[1]).y - da_dgrad(P, G[2], F[2]).y) * P.half_over_dx;
+                    const float ddy = (da_dgrad(P, G[3], F[3]).z - da_dgrad(P, G[4], F[4]).z) * P.half_over_dx;
+                    const float ddz = (da_dgrad(P, G[5], F[5]).w - da_dgrad(P, G[6], F[6]).w) * P.half_over_dx;
+                    const float a = d0.x;
+                    const float Ex = coef * cxx * d0.y * q + a * ddx * q + a * d0.y * qx;
+                    const float Ey = coef * cyy * d0.z * q + a * ddy * q + a * d0.z * qy;
+                    const float Ez = coef * czz * d0.w * q + a * ddz * q + a * d0.w * qz;
+                    lap_val += P.eps0sq * (Ex + Ey + Ez);
+                }
+                lap_sl[t] = lap_val;
+                b_sl[t] = calc_b(P, F[0].cabs);
+            }
+            // dominant solid and anisotropic solid-liquid potential (:579-595)
+            int ts = -1;
+            float maxv = -1.0f;
+            for (int t = 1; t < n; ++t)
+                if (vc[t] > maxv) { maxv = vc[t]; ts = t; }
+            if (ts > 0) {
+                const int g = ids[ts];
+                float3 gs;
+                gs.x = (lookup<S>(in, cells, pt[1], g) - lookup<S>(in, cells, pt[2], g)) * P.inv_2dx;
+                gs.y = (lookup<S>(in, cells, pt[3], g) - lookup<S>(in, cells, pt[4], g)) * P.inv_2dx;
+                gs.z = (lookup<S>(in, cells, pt[5], g) - lookup<S>(in, cells, pt[6], g)) * P.inv_2dx;
+                const Facet fs = facet(gs, n111 + (size_t)g * 24, P.g2_floor);
+                const float al = calc_a(P, fs.cabs);
+                w_sl = P.w0 * (al * al);
+            }
+        } else {
+            // isotropic branch of the switchable kernel (:729-731)
+            for (int t = 1; t < n; ++t) lap_sl[t] = P.eps0sq * lapk[0];
+        }
+    }
+
+    // pair sums (:600-661)
+    const float dT = (float)(T0z[k] - P.Tmc);
+    const float inv_n = 1.0f / (float)(n > 0 ? n : 1);
+    const int N = P.N;
+    float outv[AMAX];
+    for (int t1 = 0; t1 < n; ++t1) {
+        const int i = ids[t1];
+        float dpi = 0.0f;
+        for (int t2 = 0; t2 < n; ++t2) {
+            const int j = ids[t2];
+            if (i == j) continue;
+            const bool sl = (i != LIQ && j == LIQ), ls = (i == LIQ && j != LIQ);
+            const float df = sl ? -P.Sf * dT : (ls ? P.Sf * dT : 0.0f);
+            float ppp = 0.0f;
+            for (int t3 = 0; t3 < n; ++t3) {
+                const int q = ids[t3];
+                float wik = __ldg(wij + i * N + q), wjk = __ldg(wij + j * N + q);
+                if (q == LIQ) {
+                    if (i != LIQ) wik = w_sl;
+                    if (j != LIQ) wjk = w_sl;
+                }
+                float term2 = 0.0f;
+                if (sl) {
+                    if (q == i) term2 = 0.5f * lap_sl[t1];
+                } else if (ls) {
+                    if (q == j) term2 = -0.5f * lap_sl[t2];
+                } else {
+                    term2 = 0.5f * (__ldg(a2ij + i * N + q) - __ldg(a2ij + j * N + q)) * lapk[t3];
+                }
+                ppp += (wik - wjk) * vc[t3] + term2;
+            }
+            const float tf = FORCE_PREF * sqrtf(fmaxf(vc[t1] * vc[t2], 0.0f)) * df;
+            float me = __ldg(mij + i * N + j);
+            if (sl) me *= b_sl[t1];
+            else if (ls) me *= b_sl[t2];
+            dpi -= 2.0f * me * inv_n * (ppp - tf);
+        }
+        outv[t1] = fminf(fmaxf(vc[t1] + P.dt * dpi, 0.0f), 1.0f);
+    }
+
+    // renormalise with a compensated (TwoSum) float accumulation (:663-680)
+    float sh = 0.0f, sl_ = 0.0f;
+    for (int t = 0; t < n; ++t) {
+        const float a = sh, b = outv[t];
+        const float s = a + b;
+        const float bb = s - a;
+        sl_ += (a - (s - bb)) + (b - bb);
+        sh = s;
+    }
+    const float stot = sh + sl_;
+    int cnt_out = 0;
+    bool sovf = false;
+    if (stot > 1e-20f) {
+        float inv = 1.0f / sh;
+        inv = inv - inv * inv * sl_;
+        for (int t = 0; t < n; ++t) {
+            const float v = outv[t] * inv;
+            if (v > 0.0f) {
+                if (cnt_out < S) {
+                    out.idx[cnt_out * cells + c] = (uint16_t)ids[t];
+                    out.val[cnt_out * cells + c] = v;
+                    ++cnt_out;
+                } else {
+                    sovf = true;
+                }
+            }
+        }
+    } else {
+        // all clipped to ~0: the liquid takes the cell (:679-680)
+        out.idx[c] = LIQ;
+        out.val[c] = 1.0f;
+        cnt_out = 1;
+        for (int t = 0; t < n; ++t) {
+            if (ids[t] == LIQ || !(outv[t] > 0.0f)) continue;
+            if (cnt_out < S) {
+                out.idx[cnt_out * cells + c] = (uint16_t)ids[t];
+                out.val[cnt_out * cells + c] = outv[t];
+                ++cnt_out;
+            } else {
+                sovf = true;
+            }
+        }
+    }
+    out.cnt[c] = (uint8_t)cnt_out;
+    if (sovf) atomicOr(err, MPF3D_DEV_SLOT_OVERFLOW);
+}
+
+// ---------------------------------------------------------------------------
+// dense [N][nx][ny][nz] (z fastest) -> compact (x fastest)
+template <typename T, int S>
+__global__ void from_dense_kernel(const T *__restrict__ phi, int N, int nx, int ny, int nz, Out out,
+                                  int32_t *__restrict__ err) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int m = blockIdx.y * blockDim.y + threadIdx.y;
+    const int l = blockIdx.z * blockDim.z + threadIdx.z;
+    if (k >= nz || m >= ny || l >= nx) return;
+    const int64_t plane = (int64_t)nx * ny * nz;
+    const int64_t src = ((int64_t)l * ny + m) * nz + k;
+    const int64_t cells = plane;
+    const int64_t dst = ((int64_t)k * ny + m) * nx + l;
+    int c = 0;
+    bool bad = false, ovf = false;
+    for (int g = 0; g < N; ++g) {
+        const T v = phi[(int64_t)g * plane + src];
+        if (!(v >= (T)0)) { bad = true; continue; }
+        if (v > (T)0) {
+            if (c < S) {
+                out.idx[c * cells + dst] = (uint16_t)g;
+                out.val[c * cells + dst] = (float)v;
+            } else {
+                ovf = true;
+            }
+            ++c;
+        }
+    }
+    out.cnt[dst] = (uint8_t)(c < S ? c : S);
+    if (bad) atomicOr(err, MPF3D_DEV_BAD_INPUT);
+    if (ovf) atomicOr(err, MPF3D_DEV_SLOT_OVERFLOW);
+}
+
+template <typename T, int S>
+__global__ void to_dense_kernel(In in, int N, int nx, int ny, int nz, T *__restrict__ phi) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int m = blockIdx.y * blockDim.y + threadIdx.y;
+    const int l = blockIdx.z * blockDim.z + threadIdx.z;
+    if (k >= nz || m >= ny || l >= nx) return;
+    const int64_t plane = (int64_t)nx * ny * nz;
+    const int64_t dstc = ((int64_t)l * ny + m) * nz + k;
+    const int64_t srcc = ((int64_t)k * ny + m) * nx + l;
+    for (int g = 0; g < N; ++g) phi[(int64_t)g * plane + dstc] = (T)0;
+    int c = in.cnt[srcc];
+    c = c < S ? c : S;
+    for (int s = 0; s < c; ++s) {
+        const int g = in.idx[s * plane + srcc];
+        if (g < N) phi[(int64_t)g * plane + dstc] = (T)in.val[s * plane + srcc];
+    }
+}
+
+// number of active phases per cell (the APT's nf), dense z-fastest output
+template <int S>
+__global__ void active_count_kernel(In in, int nx, int ny, int nz, int32_t *__restrict__ nf) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int m = blockIdx.y * blockDim.y + threadIdx.y;
+    const int l = blockIdx.z * blockDim.z + threadIdx.z;
+    if (k >= nz || m >= ny || l >= nx) return;
+    const int64_t cells = (int64_t)nx * ny * nz;
+    const int lp = wrap_p(l, nx), lm = wrap_m(l, nx), mp = wrap_p(m, ny), mm = wrap_m(m, ny);
+    const int kp = clamp_p(k, nz), km = clamp_m(k, nz);
+    auto cidx = [&](int a, int b, int d) { return ((int64_t)d * ny + b) * nx + a; };
+    const int64_t pt[7] = {cidx(l, m, k), cidx(lp, m, k), cidx(lm, m, k), cidx(l, mp, k),
+                           cidx(l, mm, k), cidx(l, m, kp), cidx(l, m, km)};
+    // count distinct ids of the 7 sorted lists by repeated minimum extraction
+    int pos[7];
+    for (int p = 0; p < 7; ++p) pos[p] = 0;
+    int n = 0, last = -1;
+    while (true) {
+        int best = 1 << 30;
+        for (int p = 0; p < 7; ++p) {
+            int c = in.cnt[pt[p]];
+            c = c < S ? c : S;
+            while (pos[p] < c && (int)in.idx[pos[p] * cells + pt[p]] <= last) ++pos[p];
+            if (pos[p] < c) best = min(best, (int)in.idx[pos[p] * cells + pt[p]]);
+        }
+        if (best == (1 << 30)) break;
+        last = best;
+        ++n;
+    }
+    nf[((int64_t)l * ny + m) * nz + k] = n;
+}
+
+}  // namespace compact
+}  // namespace mpf3d
+
+using namespace mpf3d;
+using namespace mpf3d::compact;
+
+namespace {
+
+dim3 zfast_grid(int nx, int ny, int nz, dim3 b) {
+    return dim3((nz + b.x - 1) / b.x, (ny + b.y - 1) / b.y, (nx + b.z - 1) / b.z);
+}
+
+bool dims_ok(int nx, int ny, int nz) {
+    return nx > 0 && ny > 0 && nz > 0 && nx <= 65535 * 32 && ny <= 65535 * 8 && nz <= 65535 * 8 &&
+           (int64_t)nx * ny * nz < ((int64_t)1 << 40);
+}
+
+template <int S, int AMAX>
+void launch_step(const In &in, const Out &out, const double *T0z, const float *wij, const float *a2ij,
+                 const float *mij, const float *n111, const Params &P, int32_t *err, cudaStream_t s) {
+    dim3 blk(32, 4, 2);
+    dim3 grd((P.nx + 31) / 32, (P.ny + 3) / 4, (P.nz + 1) / 2);
+    step_kernel<S, AMAX><<<grd, blk, 0, s>>>(in, out, T0z, wij, a2ij, mij, n111, P, err);
+}
+
+}  // namespace
+
+extern "C" int mpf3d_compact_from_dense(const void *phi, int phi_dtype, int N, int nx, int ny, int nz, int slots,
+                                        uint8_t *cnt, uint16_t *idx, float *val, int32_t *err, void *stream) {
+    if (!phi || !cnt || !idx || !val || !err || N <= 0 || N > 65535 || !dims_ok(nx, ny, nz)) return MPF3D_ERR_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    dim3 b(32, 4, 2);
+    dim3 g = zfast_grid(nx, ny, nz, b);
+    Out o{cnt, idx, val};
+#define FD(T, SS) from_dense_kernel<T, SS><<<g, b, 0, s>>>((const T *)phi, N, nx, ny, nz, o, err)
+    if (phi_dtype == MPF3D_F32) {
+        if (slots == 4) FD(float, 4); else if (slots == 8) FD(float, 8); else if (slots == 16) FD(float, 16);
+        else return MPF3D_ERR_ARG;
+    } else if (phi_dtype == MPF3D_F64) {
+        if (slots == 4) FD(double, 4); else if (slots == 8) FD(double, 8); else if (slots == 16) FD(double, 16);
+        else return MPF3D_ERR_ARG;
+    } else {
+        return MPF3D_ERR_DTYPE;
+    }
+#undef FD
+    return cudaGetLastError() == cudaSuccess ? MPF3D_OK : MPF3D_ERR_CUDA;
+}
+
+extern "C" int mpf3d_compact_to_dense(const uint8_t *cnt, const uint16_t *idx, const float *val, int slots, int N,
+                                      int nx, int ny, int nz, void *phi, int phi_dtype, void *stream) {
+    if (!phi || !cnt || !idx || !val || N <= 0 || N > 65535 || !dims_ok(nx, ny, nz)) return MPF3D_ERR_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    dim3 b(32, 4, 2);
+    dim3 g = zfast_grid(nx, ny, nz, b);
+    In in{cnt, idx, val};
+#define TD(T, SS) to_dense_kernel<T, SS><<<g, b, 0, s>>>(in, N, nx, ny, nz, (T *)phi)
+    if (phi_dtype == MPF3D_F32) {
+        if (slots == 4) TD(float, 4); else if (slots == 8) TD(float, 8); else if (slots == 16) TD(float, 16);
+        else return MPF3D_ERR_ARG;
+    } else if (phi_dtype == MPF3D_F64) {
+        if (slots == 4) TD(double, 4); else if (slots == 8) TD(double, 8); else if (slots == 16) TD(double, 16);
+        else return MPF3D_ERR_ARG;
+    } else {
+        return MPF3D_ERR_DTYPE;
+    }
+#undef TD
+    return cudaGetLastError() == cudaSuccess ? MPF3D_OK : MPF3D_ERR_CUDA;
+}
+
+extern "C" int mpf3d_compact_active_count(const uint8_t *cnt, const uint16_t *idx, int slots, int nx, int ny, int nz,
+                                          int32_t *nf, void *stream) {
+    if (!cnt || !idx || !nf || !dims_ok(nx, ny, nz)) return MPF3D_ERR_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    dim3 b(32, 4, 2);
+    dim3 g = zfast_grid(nx, ny, nz, b);
+    In in{cnt, idx, nullptr};
+    if (slots == 4) active_count_kernel<4><<<g, b, 0, s>>>(in, nx, ny, nz, nf);
+    else if (slots == 8) active_count_kernel<8><<<g, b, 0, s>>>(in, nx, ny, nz, nf);
+    else if (slots == 16) active_count_kernel<16><<<g, b, 0, s>>>(in, nx, ny, nz, nf);
+    else return MPF3D_ERR_ARG;
+    return cudaGetLastError() == cudaSuccess ? MPF3D_OK : MPF3D_ERR_CUDA;
+}
+
+extern "C" int mpf3d_compact_step(const uint8_t *cnt, const uint16_t *idx, const float *val, uint8_t *cnt_out,
+                                  uint16_t *idx_out, float *val_out, int slots, int amax, const double *T0z,
+                                  double Tm_plus_cool, const float *wij, const float *a2ij, const float *mij,
+                                  const float *n111, int N, int nx, int ny, int nz, const mpf3d_scalars *sc,
+                                  int enable_anisotropy, int enable_torque, int32_t *err, void *stream) {
+    if (!cnt || !idx || !val || !cnt_out || !idx_out || !val_out || !T0z || !wij || !a2ij || !mij || !n111 || !sc ||
+        !err)
+        return MPF3D_ERR_ARG;
+    if (N <= 0 || N > 65535 || !dims_ok(nx, ny, nz)) return MPF3D_ERR_ARG;
+    if (cnt == cnt_out || idx == idx_out || val == val_out) return MPF3D_ERR_ARG;
+    const double *v = sc->v;
+    Params P;
+    P.nx = nx; P.ny = ny; P.nz = nz; P.N = N;
+    P.cells = (int64_t)nx * ny * nz;
+    const double dx = v[MPF3D_S_DX];
+    P.inv_dx2 = (float)(1.0 / (dx * dx));
+    P.inv_2dx = (float)(1.0 / (2.0 * dx));
+    P.half_over_dx = (float)(0.5 / dx);
+    P.inv_dx = (float)(1.0 / dx);
+    P.dt = (float)v[MPF3D_S_DT];
+    P.eps0 = (float)v[MPF3D_S_EPS0_SL];
+    P.eps0sq = (float)(v[MPF3D_S_EPS0_SL] * v[MPF3D_S_EPS0_SL]);
+    P.w0 = (float)v[MPF3D_S_W0_SL];
+    P.mu_a = (float)v[MPF3D_S_MU_A];
+    P.delta_a = (float)v[MPF3D_S_DELTA_A];
+    P.mu_da = (float)(v[MPF3D_S_MU_A] * v[MPF3D_S_DELTA_A]);
+    P.pp = (float)(v[MPF3D_S_P_ROUND] * v[MPF3D_S_P_ROUND]);
+    P.tan_a0 = (float)tan(v[MPF3D_S_A0]);
+    P.g2_floor = (float)v[MPF3D_S_G2_FLOOR];
+    P.ksi = (float)v[MPF3D_S_KSI];
+    P.theta_c = (float)v[MPF3D_S_THETA_C_RAD];
+    P.Sf = (float)v[MPF3D_S_SF];
+    P.Tmc = Tm_plus_cool;
+    P.use_aniso = enable_anisotropy != 0;
+    P.use_torque = enable_anisotropy != 0 && enable_torque != 0;
+    In in{cnt, idx, val};
+    Out out{cnt_out, idx_out, val_out};
+    cudaStream_t s = (cudaStream_t)stream;
+    if (slots == 4 && amax == 8) launch_step<4, 8>(in, out, T0z, wij, a2ij, mij, n111, P, err, s);
+    else if (slots == 8 && amax == 16) launch_step<8, 16>(in, out, T0z, wij, a2ij, mij, n111, P, err, s);
+    else if (slots == 16 && amax == 32) launch_step<16, 32>(in, out, T0z, wij, a2ij, mij, n111, P, err, s);
+    else return MPF3D_ERR_ARG;
+    return cudaGetLastError() == cudaSuccess ? MPF3D_OK : MPF3D_ERR_CUDA;
+}

@@ -1,0 +1,181 @@
+"""Compact FP32 solver: the fused one-kernel-per-step tier.
+
+``CompactSolver`` owns a double-buffered compact state on one GPU (see
+include/mpf3d.h for the layout) and advances it with ``mpf3d_compact_step``.
+It replaces the reference's driver loop (run_randommode_3d.py:267-287:
+temperature kernel, APT kernel, update kernel, buffer swap) with one launch
+per step; dense phi is only materialised on request (``to_dense``).
+
+Device memory comes from torch (plumbing only); all compute is in
+libmpf3d.so.
+"""
+
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from .inputs import Physics
+
+_SLOT_TEMPLATES = {4: 8, 8: 16, 16: 32}  # slots -> max active phases per cell
+
+
+class SlotOverflow(RuntimeError):
+    """A cell needed more slots (or active phases) than the template holds."""
+
+
+def _torch():
+    import torch
+
+    return torch
+
+
+def _scalars_from(phys_or_tuple):
+    s = _lib.Scalars()
+    if isinstance(phys_or_tuple, Physics):
+        vals = phys_or_tuple.kernel_scalars(f32=False)
+    else:
+        vals = phys_or_tuple
+    if len(vals) != 13:
+        raise ValueError("13 kernel scalars expected")
+    for i, v in enumerate(vals):
+        s.v[i] = float(v)
+    s.f32mask = 0
+    return s
+
+
+def z_profile(temp) -> np.ndarray:
+    """Temperature as a float64 z profile; 3-D fields must be uniform in x, y."""
+    t = np.asarray(temp, dtype=np.float64)
+    if t.ndim == 1:
+        return np.ascontiguousarray(t)
+    if t.ndim != 3:
+        raise ValueError("temperature must be [nz] or [nx, ny, nz]")
+    prof = t[0, 0, :]
+    if not np.array_equal(t, np.broadcast_to(prof, t.shape)):
+        raise ValueError("the compact tier takes a temperature that depends on z only")
+    return np.ascontiguousarray(prof)
+
+
+class CompactSolver:
+    def __init__(self, phi0, temp0, n111, wij, aij, mij, phys: Physics | None = None, *,
+                 scalars=None, T_melt=None, cooling_rate=None, slots: int = 8,
+                 anisotropy: bool = True, torque: bool = True, device="cuda:0"):
+        torch = _torch()
+        if slots not in _SLOT_TEMPLATES:
+            raise ValueError(f"slots must be one of {sorted(_SLOT_TEMPLATES)}")
+        self.phys = phys or Physics()
+        d = self.phys.derived()
+        self.scalars = _scalars_from(scalars if scalars is not None else self.phys)
+        self.T_melt = float(self.phys.T_melt if T_melt is None else T_melt)
+        self.cooling_rate = float(d["cooling_rate"] if cooling_rate is None else cooling_rate)
+        self.anisotropy, self.torque = bool(anisotropy), bool(torque)
+        self.device = torch.device(device)
+        phi = phi0 if isinstance(phi0, torch.Tensor) else torch.from_numpy(np.ascontiguousarray(phi0))
+        if phi.dim() != 4 or phi.dtype not in (torch.float32, torch.float64):
+            raise ValueError("phi0 must be float32/float64 [N, nx, ny, nz]")
+        self.N, self.nx, self.ny, self.nz = (int(s) for s in phi.shape)
+        self.cells = self.nx * self.ny * self.nz
+        self.slots = slots
+        self.amax = _SLOT_TEMPLATES[slots]
+        to = lambda a, dt: torch.as_tensor(np.ascontiguousarray(a), dtype=dt).to(self.device)
+        self.T0z = to(z_profile(temp0), torch.float64)
+        if self.T0z.numel() != self.nz:
+            raise ValueError("temperature profile length must equal nz")
+        for nm, a, shp in (("wij", wij, (self.N, self.N)), ("aij", aij, (self.N, self.N)),
+                           ("mij", mij, (self.N, self.N)), ("n111", n111, (self.N, 8, 3))):
+            if tuple(np.shape(a)) != shp:
+                raise ValueError(f"{nm} must have shape {shp}")
+        aij32 = np.asarray(aij, np.float32)
+        self.wij = to(np.asarray(wij, np.float32), torch.float32)
+        self.a2ij = to(aij32 * aij32, torch.float32)
+        self.mij = to(np.asarray(mij, np.float32), torch.float32)
+        self.n111 = to(np.asarray(n111, np.float32), torch.float32)
+        self.err = torch.zeros(1, dtype=torch.int32, device=self.device)
+        self.buf = [self._alloc(), self._alloc()]
+        self.cur = 0
+        self.step_count = 0
+        dphi = phi.to(self.device).contiguous()
+        self._from_dense(dphi)
+        self.check()
+
+    # -- buffers ---------------------------------------------------------------
+    def _alloc(self):
+        torch = _torch()
+        return (torch.empty(self.cells, dtype=torch.uint8, device=self.device),
+                torch.empty(self.slots * self.cells, dtype=torch.int16, device=self.device),
+                torch.empty(self.slots * self.cells, dtype=torch.float32, device=self.device))
+
+    def _stream(self):
+        return _torch().cuda.current_stream(self.device).cuda_stream or None
+
+    def _from_dense(self, dphi):
+        torch = _torch()
+        cnt, idx, val = self.buf[self.cur]
+        rc = _lib.lib().mpf3d_compact_from_dense(
+            dphi.data_ptr(), 0 if dphi.dtype == torch.float32 else 1, self.N, self.nx, self.ny,
+            self.nz, self.slots, cnt.data_ptr(), idx.data_ptr(), val.data_ptr(),
+            self.err.data_ptr(), self._stream())
+        _lib.check(rc, "compact_from_dense")
+
+    # -- stepping ---------------------------------------------------------------
+    def launch_step(self, step_index: int) -> None:
+        """Enqueue one step (no synchronisation); step_index is 1-based."""
+        src = self.buf[self.cur]
+        dst = self.buf[1 - self.cur]
+        tmc = self.T_melt + step_index * self.cooling_rate
+        rc = _lib.lib().mpf3d_compact_step(
+            src[0].data_ptr(), src[1].data_ptr(), src[2].data_ptr(), dst[0].data_ptr(),
+            dst[1].data_ptr(), dst[2].data_ptr(), self.slots, self.amax, self.T0z.data_ptr(), tmc,
+            self.wij.data_ptr(), self.a2ij.data_ptr(), self.mij.data_ptr(), self.n111.data_ptr(),
+            self.N, self.nx, self.ny, self.nz, ctypes.byref(self.scalars), int(self.anisotropy),
+            int(self.torque), self.err.data_ptr(), self._stream())
+        _lib.check(rc, "compact_step")
+        self.cur = 1 - self.cur
+
+    def step(self, n: int = 1, check: bool = True) -> None:
+        for _ in range(int(n)):
+            self.step_count += 1
+            self.launch_step(self.step_count)
+        if check:
+            self.check()
+
+    def check(self) -> None:
+        v = int(self.err.item())
+        if v:
+            self.err.zero_()
+            msg = _lib.describe_dev_error(v)
+            if v & 8:
+                raise SlotOverflow(f"compact state overflow ({msg}); use more slots")
+            raise RuntimeError(f"compact solver device error: {msg}")
+
+    # -- outputs ----------------------------------------------------------------
+    def to_dense(self, dtype=np.float32, host: bool = True):
+        torch = _torch()
+        tdt = torch.float32 if np.dtype(dtype) == np.float32 else torch.float64
+        out = torch.empty((self.N, self.nx, self.ny, self.nz), dtype=tdt, device=self.device)
+        cnt, idx, val = self.buf[self.cur]
+        rc = _lib.lib().mpf3d_compact_to_dense(cnt.data_ptr(), idx.data_ptr(), val.data_ptr(),
+                                               self.slots, self.N, self.nx, self.ny, self.nz,
+                                               out.data_ptr(), 0 if tdt == torch.float32 else 1,
+                                               self._stream())
+        _lib.check(rc, "compact_to_dense")
+        return out.cpu().numpy() if host else out
+
+    def active_count(self, host: bool = True):
+        torch = _torch()
+        nf = torch.empty((self.nx, self.ny, self.nz), dtype=torch.int32, device=self.device)
+        cnt, idx, _ = self.buf[self.cur]
+        rc = _lib.lib().mpf3d_compact_active_count(cnt.data_ptr(), idx.data_ptr(), self.slots,
+                                                   self.nx, self.ny, self.nz, nf.data_ptr(),
+                                                   self._stream())
+        _lib.check(rc, "compact_active_count")
+        return nf.cpu().numpy() if host else nf
+
+    def stored_counts(self):
+        return self.buf[self.cur][0]
+
+    def state_bytes(self) -> int:
+        return self.cells * (1 + 6 * self.slots)

@@ -1,0 +1,78 @@
+"""Compact FP32 fused stepper against the FP64 oracle (reference numerics
+with float64 phi and scalars).  Tolerance: max|dphi| <= 1e-4, the FP32 bar
+of the hot path; active-phase lists of the initial state exact."""
+import numpy as np
+import pytest
+
+import oracle as O
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+TOL = 1e-4
+
+
+def oracle_fp64(case, steps, aniso=True, torque=True):
+    phi0 = case.phi.astype(np.float64)
+    temp0 = case.temp.astype(np.float64)
+    sc = O.make_scalars([float(v) for v in case.phys.kernel_scalars(f32=False)], False)
+    rate = case.phys.derived()["cooling_rate"]
+    phi, _, nf, _ = O.run(phi0, temp0, case.wij, case.aij, case.mij, case.n111, sc, steps,
+                          cooling_rate=rate, rate_f32=False, switchable=True, aniso=int(aniso),
+                          torque=int(torque))
+    return phi, nf
+
+
+def make_solver(case, **kw):
+    from mpf3d.solver import CompactSolver
+    return CompactSolver(case.phi, case.temp, case.n111, case.wij, case.aij, case.mij, case.phys, **kw)
+
+
+def test_dense_compact_round_trip_is_exact():
+    from mpf3d import inputs
+    case = inputs.voronoi_case(20, 12, 18, 6, 6, seed=2)
+    s = make_solver(case)
+    back = s.to_dense()
+    assert np.array_equal(back, case.phi)
+    nf = s.active_count()
+    mf = np.zeros((50,) + case.phi.shape[1:], np.int32)
+    onf = np.zeros(case.phi.shape[1:], np.int32)
+    O.apt(case.phi, mf, onf, np.zeros(2, np.int32))
+    assert np.array_equal(nf, onf)
+
+
+@pytest.mark.parametrize("aniso,torque", [(True, True), (True, False), (False, False)])
+def test_fp32_step_matches_fp64_oracle(aniso, torque):
+    from mpf3d import inputs
+    case = inputs.voronoi_case(24, 16, 24, 6, 8, seed=4, orientation_seed=9)
+    steps = 5
+    ref, ref_nf = oracle_fp64(case, steps, aniso, torque)
+    s = make_solver(case, anisotropy=aniso, torque=torque)
+    s.step(steps)
+    got = s.to_dense(np.float64)
+    err = np.abs(got - ref).max()
+    assert err <= TOL, f"max|dphi| = {err:.3e}"
+    assert np.abs(got.sum(axis=0) - 1.0).max() < 1e-5
+
+
+def test_fp32_undercooled_junctions():
+    from mpf3d import inputs
+    case = inputs.voronoi_case(20, 20, 20, 10, 8, seed=7, orientation_seed=3, undercooling=3.0)
+    steps = 4
+    ref, _ = oracle_fp64(case, steps)
+    s = make_solver(case)
+    s.step(steps)
+    err = np.abs(s.to_dense(np.float64) - ref).max()
+    assert err <= TOL, f"max|dphi| = {err:.3e}"
+
+
+def test_slot_overflow_is_reported():
+    from mpf3d import inputs
+    from mpf3d.solver import SlotOverflow
+    phi = np.zeros((7, 6, 6, 6), np.float32)
+    phi[1:, 2, 2, 2] = 1.0 / 6.0
+    phi[0] = np.clip(1.0 - phi[1:].sum(axis=0), 0.0, 1.0)
+    case = inputs.voronoi_case(6, 6, 6, 6, 3, seed=1)
+    with pytest.raises(SlotOverflow):
+        make_solver(inputs.Case(phi, case.temp, case.quats, case.n111, case.wij, case.aij, case.mij),
+                    slots=4)
