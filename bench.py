@@ -296,7 +296,7 @@ def run_ours(args, rank, world):
         cpu = {"value": v, "unit": UNIT, "cores": th, "kind": "port",
                "sample": f"64x64x256 crop of the workload (N=65), {st} oracle steps (reference "
                          f"float32 typing), OpenMP"}
-    emit(args, rank, world, ms, cells, t_e2e, in_bytes, out_bytes, achieved, peak, peak_kind,
+    emit(args, rank, world, value, ms, cells, t_e2e, in_bytes, out_bytes, achieved, peak, peak_kind,
          traffic, bytes_per_launch, occ, clk, cpu, final_cnt_sum)
 
 
@@ -325,7 +325,7 @@ def e2e_run(args, phi0, temp, n111, wij, aij, mij, phys, dev, barrier, world):
     return t_e2e, in_bytes, out_bytes
 
 
-def emit(args, rank, world, ms, cells, t_e2e, in_bytes, out_bytes, achieved, peak, peak_kind,
+def emit(args, rank, world, value, ms, cells, t_e2e, in_bytes, out_bytes, achieved, peak, peak_kind,
          traffic, bytes_per_launch, occ, clk, cpu, final_cnt_sum):
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -340,7 +340,7 @@ def emit(args, rank, world, ms, cells, t_e2e, in_bytes, out_bytes, achieved, pea
                              "frac": achieved / peak, "traffic": traffic,
                              "peak_source": peak_kind,
                              "bytes_per_cell_step": bytes_per_launch / cells,
-                             "kernel": "mpf3d::compact::step_kernel<8,16>"},
+                             "kernel": f"mpf3d::compact::step_kernel<{args.slots},{2 * args.slots}>"},
                 "stored_phases_per_cell": {"start": occ[0] / cells, "end": occ[-1] / cells},
                 "clocks": clk.summary(),
                 "cpu_baseline": cpu}
@@ -354,7 +354,7 @@ def main():
     ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--slots", type=int, default=8)
+    ap.add_argument("--slots", type=int, default=16)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end run (profiling)")
     ap.add_argument("--grid", type=int, nargs=3, default=None,

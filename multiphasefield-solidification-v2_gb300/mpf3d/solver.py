@@ -135,12 +135,44 @@ class CompactSolver:
         _lib.check(rc, "compact_step")
         self.cur = 1 - self.cur
 
-    def step(self, n: int = 1, check: bool = True) -> None:
-        for _ in range(int(n)):
-            self.step_count += 1
-            self.launch_step(self.step_count)
-        if check:
+    def step(self, n: int = 1, check: bool = True, check_every: int = 200) -> None:
+        """Advance n steps.  With check=True the device error word is read
+        every `check_every` steps; a slot overflow rolls the state back to the
+        start of that chunk, widens the slot template (4 -> 8 -> 16) and
+        redoes the chunk, so no phase is ever dropped silently."""
+        n = int(n)
+        if not check:
+            for _ in range(n):
+                self.step_count += 1
+                self.launch_step(self.step_count)
+            return
+        done = 0
+        while done < n:
+            chunk = min(int(check_every), n - done)
+            ckpt = [t.clone() for t in self.buf[self.cur]], self.step_count
+            for _ in range(chunk):
+                self.step_count += 1
+                self.launch_step(self.step_count)
+            v = int(self.err.item())
+            if v & 8 and self.slots < max(_SLOT_TEMPLATES):
+                self.err.zero_()
+                self._restore_widened(ckpt)
+                continue
             self.check()
+            done += chunk
+
+    def _restore_widened(self, ckpt) -> None:
+        (cnt, idx, val), steps = ckpt
+        old = self.slots
+        self.slots = {4: 8, 8: 16}[old]
+        self.amax = _SLOT_TEMPLATES[self.slots]
+        self.buf = [self._alloc(), self._alloc()]
+        self.cur = 0
+        c2, i2, v2 = self.buf[0]
+        c2.copy_(cnt)
+        i2[: old * self.cells].copy_(idx)
+        v2[: old * self.cells].copy_(val)
+        self.step_count = steps
 
     def check(self) -> None:
         v = int(self.err.item())

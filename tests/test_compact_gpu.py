@@ -76,3 +76,15 @@ def test_slot_overflow_is_reported():
     with pytest.raises(SlotOverflow):
         make_solver(inputs.Case(phi, case.temp, case.quats, case.n111, case.wij, case.aij, case.mij),
                     slots=4)
+
+
+def test_slot_template_widens_instead_of_dropping_phases():
+    """Start with 4 slots on a junction-rich case: the solver must widen its
+    template and give the same result as a run that started with 16."""
+    from mpf3d import inputs
+    case = inputs.voronoi_case(20, 20, 16, 12, 6, seed=5, orientation_seed=2, undercooling=2.0)
+    a = make_solver(case, slots=4)
+    a.step(6, check_every=3)
+    b = make_solver(case, slots=16)
+    b.step(6)
+    assert np.array_equal(a.to_dense(), b.to_dense())
