@@ -154,15 +154,32 @@ __device__ __forceinline__ float4 da_dgrad(const Params &P, float3 g, const Face
                        coef * (f.nz * ig - ud * g.z * ig3));
 }
 
-template <int S, int AMAX>
-__global__ void __launch_bounds__(256) step_kernel(In in, Out out, const double *__restrict__ T0z,
-                                                   const float *__restrict__ wij, const float *__restrict__ a2ij,
-                                                   const float *__restrict__ mij, const float *__restrict__ n111,
-                                                   Params P, int32_t *__restrict__ err) {
-    const int l = blockIdx.x * blockDim.x + threadIdx.x;
-    const int m = blockIdx.y * blockDim.y + threadIdx.y;
-    const int k = blockIdx.z * blockDim.z + threadIdx.z;
-    if (l >= P.nx || m >= P.ny || k >= P.nz) return;
+// Work list of solid-liquid interface cells for the second kernel of a
+// step (scratch memory owned by the caller): items[] holds x-fastest cell
+// indices, count[2] two counters used on alternate steps so that no memset
+// is needed between steps.
+struct Queue {
+    uint32_t *__restrict__ items;
+    uint32_t *__restrict__ count;
+};
+
+struct Mats {
+    const double *__restrict__ T0z;
+    const float *__restrict__ wij;
+    const float *__restrict__ a2ij;
+    const float *__restrict__ mij;
+    const float *__restrict__ n111;
+};
+
+// General update of one cell (the path of non-uniform neighbourhoods).
+// HEAVY enables the anisotropic interface, torque and kinetic terms.
+template <int S, int AMAX, bool HEAVY>
+__device__ __forceinline__ void process_cell(const In &in, const Out &out, const Mats &M, const Params &P,
+                                             int32_t *__restrict__ err, int l, int m, int k) {
+    const float *__restrict__ wij = M.wij;
+    const float *__restrict__ a2ij = M.a2ij;
+    const float *__restrict__ mij = M.mij;
+    const float *__restrict__ n111 = M.n111;
     const int64_t cells = P.cells;
     const int lp = wrap_p(l, P.nx), lm = wrap_m(l, P.nx), mp = wrap_p(m, P.ny), mm = wrap_m(m, P.ny);
     const int kp = clamp_p(k, P.nz), km = clamp_m(k, P.nz);
@@ -175,23 +192,7 @@ __global__ void __launch_bounds__(256) step_kernel(In in, Out out, const double 
     pt[5] = cell_of(P, l, m, kp);
     pt[6] = cell_of(P, l, m, km);
     const int64_t c = pt[0];
-
-    // fast path: the cell and its 6 neighbours hold one and the same phase.
-    // Then the active list is that phase alone, the pair sums are empty and
-    // the renormalised fraction is exactly 1.
     const int c0 = __ldg(in.cnt + c);
-    const int i0 = __ldg(in.idx + c);
-    bool uniform = (c0 == 1);
-#pragma unroll
-    for (int p = 1; p < 7; ++p)
-        uniform = uniform && (__ldg(in.cnt + pt[p]) == 1) && (__ldg(in.idx + pt[p]) == i0);
-    if (uniform) {
-        out.cnt[c] = 1;
-        out.idx[c] = (uint16_t)i0;
-        out.val[c] = 1.0f;
-        return;
-    }
-
     // active list: ascending union of the 7 stored lists (the APT rule of
     // kernel_update_nfmf_3d for phi >= 0)
     int ids[AMAX];
@@ -250,7 +251,7 @@ __global__ void __launch_bounds__(256) step_kernel(In in, Out out, const double 
         b_sl[t] = 1.0f;
     }
     if (has_liq && has_solid) {
-        if (P.use_aniso) {
+        if (HEAVY && P.use_aniso) {
             const int pl[7] = {l, lp, lm, l, l, l, l};
             const int pm[7] = {m, m, m, mp, mm, m, m};
             const int pk[7] = {k, k, k, k, k, kp, km};
@@ -345,7 +346,7 @@ __global__ void __launch_bounds__(256) step_kernel(In in, Out out, const double 
     }
 
     // pair sums (:600-661)
-    const float dT = (float)(T0z[k] - P.Tmc);
+    const float dT = (float)(M.T0z[k] - P.Tmc);
     const float inv_n = 1.0f / (float)(n > 0 ? n : 1);
     const int N = P.N;
     float outv[AMAX];
@@ -429,6 +430,78 @@ __global__ void __launch_bounds__(256) step_kernel(In in, Out out, const double 
     }
     out.cnt[c] = (uint8_t)cnt_out;
     if (sovf) atomicOr(err, MPF3D_DEV_SLOT_OVERFLOW);
+}
+
+// Kernel 1 of a step: every cell.  Uniform neighbourhoods (the cell and its
+// 6 neighbours hold one and the same phase: active list of one phase, empty
+// pair sums, renormalised fraction exactly 1) are written directly;
+// neighbourhoods holding both liquid and a solid are queued for kernel 2
+// when anisotropy is on; all others (grain boundaries, junctions without
+// liquid, the isotropic model) are updated here.
+template <int S, int AMAX>
+__global__ void __launch_bounds__(256) sweep_kernel(In in, Out out, Mats M, Params P, Queue Q, int parity,
+                                                    int32_t *__restrict__ err) {
+    const int l = blockIdx.x * blockDim.x + threadIdx.x;
+    const int m = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z * blockDim.z + threadIdx.z;
+    if (blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.x == 0 && threadIdx.y == 0 &&
+        threadIdx.z == 0)
+        Q.count[parity ^ 1] = 0;  // kernel 2 of the previous step has finished with it
+    if (l >= P.nx || m >= P.ny || k >= P.nz) return;
+    const int lp = wrap_p(l, P.nx), lm = wrap_m(l, P.nx), mp = wrap_p(m, P.ny), mm = wrap_m(m, P.ny);
+    const int kp = clamp_p(k, P.nz), km = clamp_m(k, P.nz);
+    const int64_t c = cell_of(P, l, m, k);
+    const int64_t nb[6] = {cell_of(P, lp, m, k), cell_of(P, lm, m, k), cell_of(P, l, mp, k),
+                           cell_of(P, l, mm, k), cell_of(P, l, m, kp), cell_of(P, l, m, km)};
+    const int c0 = __ldg(in.cnt + c);
+    const int i0 = __ldg(in.idx + c);
+    bool uniform = (c0 == 1);
+    bool liq = c0 > 0 && i0 == LIQ;
+    bool sol = c0 > 1 || (c0 == 1 && i0 != LIQ);
+#pragma unroll
+    for (int p = 0; p < 6; ++p) {
+        const int cq = __ldg(in.cnt + nb[p]);
+        const int iq = __ldg(in.idx + nb[p]);
+        uniform = uniform && cq == 1 && iq == i0;
+        liq = liq || (cq > 0 && iq == LIQ);
+        sol = sol || cq > 1 || (cq == 1 && iq != LIQ);
+    }
+    if (uniform) {
+        out.cnt[c] = 1;
+        out.idx[c] = (uint16_t)i0;
+        out.val[c] = 1.0f;
+        return;
+    }
+    const bool push = liq && sol && P.use_aniso;
+    const unsigned am = __activemask();
+    const unsigned bm = __ballot_sync(am, push);
+    if (bm) {
+        const int lane = threadIdx.x & 31;
+        const int leader = __ffs(bm) - 1;
+        uint32_t base = 0;
+        if (lane == leader) base = atomicAdd(Q.count + parity, (uint32_t)__popc(bm));
+        base = __shfl_sync(am, base, leader);
+        if (push) Q.items[base + __popc(bm & ((1u << lane) - 1u))] = (uint32_t)c;
+    }
+    if (push) return;
+    process_cell<S, AMAX, false>(in, out, M, P, err, l, m, k);
+}
+
+// Kernel 2 of a step: the queued solid-liquid interface cells, one thread
+// per cell, all lanes of a warp on the same (heavy) path.
+template <int S, int AMAX>
+__global__ void __launch_bounds__(128) interface_kernel(In in, Out out, Mats M, Params P, Queue Q, int parity,
+                                                        int32_t *__restrict__ err) {
+    const uint32_t n = *(volatile uint32_t *)(Q.count + parity);
+    const uint32_t plane = (uint32_t)P.nx * (uint32_t)P.ny;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t c = Q.items[i];
+        const int k = (int)(c / plane);
+        const uint32_t r = c - (uint32_t)k * plane;
+        const int m = (int)(r / (uint32_t)P.nx);
+        const int l = (int)(r - (uint32_t)m * (uint32_t)P.nx);
+        process_cell<S, AMAX, true>(in, out, M, P, err, l, m, k);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -532,11 +605,17 @@ bool dims_ok(int nx, int ny, int nz) {
 }
 
 template <int S, int AMAX>
-void launch_step(const In &in, const Out &out, const double *T0z, const float *wij, const float *a2ij,
-                 const float *mij, const float *n111, const Params &P, int32_t *err, cudaStream_t s) {
+void launch_step(const In &in, const Out &out, const Mats &M, const Params &P, const Queue &Q, int parity,
+                 int32_t *err, cudaStream_t s) {
     dim3 blk(32, 4, 2);
     dim3 grd((P.nx + 31) / 32, (P.ny + 3) / 4, (P.nz + 1) / 2);
-    step_kernel<S, AMAX><<<grd, blk, 0, s>>>(in, out, T0z, wij, a2ij, mij, n111, P, err);
+    sweep_kernel<S, AMAX><<<grd, blk, 0, s>>>(in, out, M, P, Q, parity, err);
+    if (P.use_aniso) {
+        int dev = 0, sms = 148;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        interface_kernel<S, AMAX><<<sms * 8, 128, 0, s>>>(in, out, M, P, Q, parity, err);
+    }
 }
 
 }  // namespace
@@ -601,11 +680,13 @@ extern "C" int mpf3d_compact_step(const uint8_t *cnt, const uint16_t *idx, const
                                   uint16_t *idx_out, float *val_out, int slots, int amax, const double *T0z,
                                   double Tm_plus_cool, const float *wij, const float *a2ij, const float *mij,
                                   const float *n111, int N, int nx, int ny, int nz, const mpf3d_scalars *sc,
-                                  int enable_anisotropy, int enable_torque, int32_t *err, void *stream) {
+                                  int enable_anisotropy, int enable_torque, uint32_t *work_items,
+                                  uint32_t *work_count, int parity, int32_t *err, void *stream) {
     if (!cnt || !idx || !val || !cnt_out || !idx_out || !val_out || !T0z || !wij || !a2ij || !mij || !n111 || !sc ||
-        !err)
+        !err || !work_items || !work_count)
         return MPF3D_ERR_ARG;
     if (N <= 0 || N > 65535 || !dims_ok(nx, ny, nz)) return MPF3D_ERR_ARG;
+    if ((int64_t)nx * ny * nz >= ((int64_t)1 << 31)) return MPF3D_ERR_TOO_LARGE;
     if (cnt == cnt_out || idx == idx_out || val == val_out) return MPF3D_ERR_ARG;
     const double *v = sc->v;
     Params P;
@@ -634,10 +715,13 @@ extern "C" int mpf3d_compact_step(const uint8_t *cnt, const uint16_t *idx, const
     P.use_torque = enable_anisotropy != 0 && enable_torque != 0;
     In in{cnt, idx, val};
     Out out{cnt_out, idx_out, val_out};
+    Mats M{T0z, wij, a2ij, mij, n111};
+    Queue Q{work_items, work_count};
+    parity &= 1;
     cudaStream_t s = (cudaStream_t)stream;
-    if (slots == 4 && amax == 8) launch_step<4, 8>(in, out, T0z, wij, a2ij, mij, n111, P, err, s);
-    else if (slots == 8 && amax == 16) launch_step<8, 16>(in, out, T0z, wij, a2ij, mij, n111, P, err, s);
-    else if (slots == 16 && amax == 32) launch_step<16, 32>(in, out, T0z, wij, a2ij, mij, n111, P, err, s);
+    if (slots == 4 && amax == 8) launch_step<4, 8>(in, out, M, P, Q, parity, err, s);
+    else if (slots == 8 && amax == 16) launch_step<8, 16>(in, out, M, P, Q, parity, err, s);
+    else if (slots == 16 && amax == 32) launch_step<16, 32>(in, out, M, P, Q, parity, err, s);
     else return MPF3D_ERR_ARG;
     return cudaGetLastError() == cudaSuccess ? MPF3D_OK : MPF3D_ERR_CUDA;
 }

@@ -94,6 +94,9 @@ class CompactSolver:
         self.mij = to(np.asarray(mij, np.float32), torch.float32)
         self.n111 = to(np.asarray(n111, np.float32), torch.float32)
         self.err = torch.zeros(1, dtype=torch.int32, device=self.device)
+        # scratch of the step: interface work list and its two counters
+        self.work_items = torch.empty(self.cells, dtype=torch.int32, device=self.device)
+        self.work_count = torch.zeros(2, dtype=torch.int32, device=self.device)
         self.buf = [self._alloc(), self._alloc()]
         self.cur = 0
         self.step_count = 0
@@ -131,7 +134,8 @@ class CompactSolver:
             dst[1].data_ptr(), dst[2].data_ptr(), self.slots, self.amax, self.T0z.data_ptr(), tmc,
             self.wij.data_ptr(), self.a2ij.data_ptr(), self.mij.data_ptr(), self.n111.data_ptr(),
             self.N, self.nx, self.ny, self.nz, ctypes.byref(self.scalars), int(self.anisotropy),
-            int(self.torque), self.err.data_ptr(), self._stream())
+            int(self.torque), self.work_items.data_ptr(), self.work_count.data_ptr(),
+            step_index & 1, self.err.data_ptr(), self._stream())
         _lib.check(rc, "compact_step")
         self.cur = 1 - self.cur
 
@@ -168,6 +172,7 @@ class CompactSolver:
         self.amax = _SLOT_TEMPLATES[self.slots]
         self.buf = [self._alloc(), self._alloc()]
         self.cur = 0
+        self.work_count.zero_()
         c2, i2, v2 = self.buf[0]
         c2.copy_(cnt)
         i2[: old * self.cells].copy_(idx)
