@@ -33,6 +33,8 @@ constexpr float FORCE_PREF = (float)(8.0 / 3.1415926535);
 struct Params {
     int nx, ny, nz, N;
     int64_t cells;
+    uint32_t cells32;
+    float e2_flat, b_flat;  // eps^2 and b for a liquid gradient below the floor
     float inv_dx2, inv_2dx, half_over_dx, inv_dx, dt;
     float eps0, eps0sq, w0, mu_a, delta_a, mu_da, pp, tan_a0, g2_floor, ksi, theta_c, Sf;
     double Tmc;  // T_melt + accumulated cooling (float64)
@@ -171,241 +173,297 @@ struct Mats {
     const float *__restrict__ n111;
 };
 
-// General update of one cell (the path of non-uniform neighbourhoods).
-// HEAVY enables the anisotropic interface, torque and kinetic terms.
+__device__ __forceinline__ uint32_t cidx(const Params &P, int l, int m, int k) {
+    return ((uint32_t)k * (uint32_t)P.ny + (uint32_t)m) * (uint32_t)P.nx + (uint32_t)l;
+}
+
+__device__ __forceinline__ float liquid32(const In &in, uint32_t q) {
+    const int c = __ldg(in.cnt + q);
+    if (c == 0 || __ldg(in.idx + q) != LIQ) return 0.0f;
+    return __ldg(in.val + q);
+}
+
+// Active list of one cell: the ascending union of the stored lists of the
+// cell and its 6 neighbours (the APT rule of kernel_update_nfmf_3d for
+// phi >= 0), produced by a 7-way merge of the sorted lists, which also
+// yields every active phase's value at the 7 points without any search.
+template <int AMAX>
+struct Active {
+    int n;
+    bool ovf;
+    int ids[AMAX];
+    float vc[AMAX];   // value at the cell
+    float lap[AMAX];  // 7-point Laplacian (laplacian_3d :444-459)
+    float vL[7];      // liquid at the 7 points
+    int ts;           // index of the dominant solid (max value at the cell), -1 if none
+    float3 gs;        // its gradient at the cell
+};
+
+template <int S, int AMAX>
+__device__ __forceinline__ void gather(const In &in, const Params &P, const uint32_t (&pt)[7], Active<AMAX> &A) {
+    const uint32_t cells = P.cells32;
+    int cnt[7], pos[7], head[7];
+#pragma unroll
+    for (int p = 0; p < 7; ++p) {
+        const int c = __ldg(in.cnt + pt[p]);
+        cnt[p] = c < S ? c : S;
+        pos[p] = 0;
+        head[p] = cnt[p] > 0 ? (int)__ldg(in.idx + pt[p]) : 0x7fffffff;
+        A.vL[p] = 0.0f;
+    }
+    A.n = 0;
+    A.ovf = false;
+    A.ts = -1;
+    A.gs = make_float3(0.f, 0.f, 0.f);
+    float maxv = -1.0f;
+    while (true) {
+        int id = head[0];
+#pragma unroll
+        for (int p = 1; p < 7; ++p) id = min(id, head[p]);
+        if (id == 0x7fffffff) break;
+        float v[7];
+#pragma unroll
+        for (int p = 0; p < 7; ++p) {
+            v[p] = 0.0f;
+            if (head[p] == id) {
+                v[p] = __ldg(in.val + (uint32_t)pos[p] * cells + pt[p]);
+                ++pos[p];
+                head[p] = pos[p] < cnt[p] ? (int)__ldg(in.idx + (uint32_t)pos[p] * cells + pt[p]) : 0x7fffffff;
+            }
+        }
+        if (A.n == AMAX) {
+            A.ovf = true;
+            break;
+        }
+        A.ids[A.n] = id;
+        A.vc[A.n] = v[0];
+        A.lap[A.n] = (v[1] + v[2] + v[3] + v[4] + v[5] + v[6] - 6.0f * v[0]) * P.inv_dx2;
+        if (id == LIQ) {
+#pragma unroll
+            for (int p = 0; p < 7; ++p) A.vL[p] = v[p];
+        } else if (v[0] > maxv) {
+            maxv = v[0];
+            A.ts = A.n;
+            A.gs = make_float3((v[1] - v[2]) * P.inv_2dx, (v[3] - v[4]) * P.inv_2dx, (v[5] - v[6]) * P.inv_2dx);
+        }
+        ++A.n;
+    }
+}
+
+// eps^2-weighted divergence, torque and kinetic factor of one solid grain at
+// a cell from the liquid gradient at the 7 points and the liquid's second
+// derivatives at the cell (aniso_term1_solid_3d :149-204, torque_A11_3d
+// :386-441, A13_divergence_3d :344-383, calc_b_from_cos :33-55).
+__device__ __forceinline__ void interface_terms(const Params &P, const float3 (&G)[7], const float (&vL)[7],
+                                                const float (&h2)[6], const float *__restrict__ u, bool torque,
+                                                float &lap_sl, float &b_sl) {
+    Facet F[7];
+    bool any = false;
+#pragma unroll
+    for (int p = 0; p < 7; ++p) {
+        F[p] = facet(G[p], u, P.g2_floor);
+        any = any || F[p].valid;
+    }
+    const float Lc = vL[0];
+    const float h = P.inv_2dx * P.inv_dx;
+    if (!any) {
+        // flat liquid everywhere: eps^2 = (eps0 a(0))^2 at all 7 points, no torque
+        const float e2 = P.e2_flat;
+        lap_sl = ((2.0f * e2) * (vL[1] - Lc) - (2.0f * e2) * (Lc - vL[2])) * h +
+                 ((2.0f * e2) * (vL[3] - Lc) - (2.0f * e2) * (Lc - vL[4])) * h +
+                 ((2.0f * e2) * (vL[5] - Lc) - (2.0f * e2) * (Lc - vL[6])) * h;
+        b_sl = P.b_flat;
+        return;
+    }
+    float e2[7];
+#pragma unroll
+    for (int p = 0; p < 7; ++p) {
+        const float e = P.eps0 * calc_a(P, F[p].cabs);
+        e2[p] = F[p].valid ? e * e : P.e2_flat;
+    }
+    float lv = ((e2[0] + e2[1]) * (vL[1] - Lc) - (e2[0] + e2[2]) * (Lc - vL[2])) * h +
+               ((e2[0] + e2[3]) * (vL[3] - Lc) - (e2[0] + e2[4]) * (Lc - vL[4])) * h +
+               ((e2[0] + e2[5]) * (vL[5] - Lc) - (e2[0] + e2[6]) * (Lc - vL[6])) * h;
+    if (torque && F[0].valid) {
+        const float3 g0 = G[0];
+        const float q = F[0].q;
+        const float pxx = h2[0], pyy = h2[1], pzz = h2[2], pxy = h2[3], pxz = h2[4], pyz = h2[5];
+        const float qx = 2.0f * (g0.x * pxx + g0.y * pxy + g0.z * pxz);
+        const float qy = 2.0f * (g0.x * pxy + g0.y * pyy + g0.z * pyz);
+        const float qz = 2.0f * (g0.x * pxz + g0.y * pyz + g0.z * pzz);
+        const float4 d0 = da_dgrad(P, g0, F[0]);
+        const float ig = rsqrtf(q), ig3 = ig * ig * ig;
+        const float ud = g0.x * F[0].nx + g0.y * F[0].ny + g0.z * F[0].nz;
+        const float dcx = F[0].nx * ig - ud * g0.x * ig3;
+        const float dcy = F[0].ny * ig - ud * g0.y * ig3;
+        const float dcz = F[0].nz * ig - ud * g0.z * ig3;
+        const float cxx = dcx * pxx + dcy * pxy + dcz * pxz;
+        const float cyy = dcx * pxy + dcy * pyy + dcz * pyz;
+        const float czz = dcx * pxz + dcy * pyz + dcz * pzz;
+        const float cs = F[0].cs, cs2 = cs * cs;
+        const float coef = P.mu_da * (cs / sqrtf(cs2 + P.pp) - P.tan_a0 * (cs / sqrtf(fmaxf(1.0f - cs2, 0.0f) + P.pp)));
+        const float ddx = (da_dgrad(P, G[1], F[1]).y - da_dgrad(P, G[2], F[2]).y) * P.half_over_dx;
+        const float ddy = (da_dgrad(P, G[3], F[3]).z - da_dgrad(P, G[4], F[4]).z) * P.half_over_dx;
+        const float ddz = (da_dgrad(P, G[5], F[5]).w - da_dgrad(P, G[6], F[6]).w) * P.half_over_dx;
+        const float a = d0.x;
+        const float Ex = coef * cxx * d0.y * q + a * ddx * q + a * d0.y * qx;
+        const float Ey = coef * cyy * d0.z * q + a * ddy * q + a * d0.z * qy;
+        const float Ez = coef * czz * d0.w * q + a * ddz * q + a * d0.w * qz;
+        lv += P.eps0sq * (Ex + Ey + Ez);
+    }
+    lap_sl = lv;
+    b_sl = calc_b(P, F[0].cabs);
+}
+
+// Update of one cell whose neighbourhood is not uniform.  HEAVY enables the
+// anisotropic solid-liquid terms (cells with liquid and a solid active).
 template <int S, int AMAX, bool HEAVY>
 __device__ __forceinline__ void process_cell(const In &in, const Out &out, const Mats &M, const Params &P,
                                              int32_t *__restrict__ err, int l, int m, int k) {
-    const float *__restrict__ wij = M.wij;
-    const float *__restrict__ a2ij = M.a2ij;
-    const float *__restrict__ mij = M.mij;
-    const float *__restrict__ n111 = M.n111;
-    const int64_t cells = P.cells;
+    const uint32_t cells = P.cells32;
     const int lp = wrap_p(l, P.nx), lm = wrap_m(l, P.nx), mp = wrap_p(m, P.ny), mm = wrap_m(m, P.ny);
     const int kp = clamp_p(k, P.nz), km = clamp_m(k, P.nz);
-    int64_t pt[7];
-    pt[0] = cell_of(P, l, m, k);
-    pt[1] = cell_of(P, lp, m, k);
-    pt[2] = cell_of(P, lm, m, k);
-    pt[3] = cell_of(P, l, mp, k);
-    pt[4] = cell_of(P, l, mm, k);
-    pt[5] = cell_of(P, l, m, kp);
-    pt[6] = cell_of(P, l, m, km);
-    const int64_t c = pt[0];
-    const int c0 = __ldg(in.cnt + c);
-    // active list: ascending union of the 7 stored lists (the APT rule of
-    // kernel_update_nfmf_3d for phi >= 0)
-    int ids[AMAX];
-    int n = 0;
-    bool ovf = false;
-    for (int p = 0; p < 7; ++p) {
-        const int64_t q = pt[p];
-        int cq = __ldg(in.cnt + q);
-        cq = cq < S ? cq : S;
-        for (int s = 0; s < cq; ++s) {
-            const int id = __ldg(in.idx + s * cells + q);
-            int pos = n;
-            bool dup = false;
-            for (int j = 0; j < n; ++j) {
-                if (ids[j] == id) { dup = true; break; }
-                if (ids[j] > id) { pos = j; break; }
-            }
-            if (dup) continue;
-            if (n == AMAX) { ovf = true; continue; }
-            for (int j = n; j > pos; --j) ids[j] = ids[j - 1];
-            ids[pos] = id;
-            ++n;
-        }
-    }
-    if (ovf) {
-        // leave the cell as it was and report; the host re-runs the step
-        // with a wider template
+    const uint32_t pt[7] = {cidx(P, l, m, k), cidx(P, lp, m, k), cidx(P, lm, m, k), cidx(P, l, mp, k),
+                            cidx(P, l, mm, k), cidx(P, l, m, kp), cidx(P, l, m, km)};
+    const uint32_t c = pt[0];
+    Active<AMAX> A;
+    gather<S, AMAX>(in, P, pt, A);
+    if (A.ovf) {
+        // leave the cell as it was and report; the host re-runs the step with
+        // a wider template
         atomicOr(err, MPF3D_DEV_SLOT_OVERFLOW);
-        out.cnt[c] = (uint8_t)(c0 < S ? c0 : S);
-        for (int s = 0; s < c0 && s < S; ++s) {
-            out.idx[s * cells + c] = __ldg(in.idx + s * cells + c);
-            out.val[s * cells + c] = __ldg(in.val + s * cells + c);
+        const int c0 = min((int)__ldg(in.cnt + c), S);
+        out.cnt[c] = (uint8_t)c0;
+        for (int s = 0; s < c0; ++s) {
+            out.idx[(uint32_t)s * cells + c] = __ldg(in.idx + (uint32_t)s * cells + c);
+            out.val[(uint32_t)s * cells + c] = __ldg(in.val + (uint32_t)s * cells + c);
         }
         return;
     }
-
-    float vc[AMAX], lapk[AMAX];
-    for (int t = 0; t < n; ++t) {
-        const int id = ids[t];
-        const float v = lookup<S>(in, cells, c, id);
-        float s6 = lookup<S>(in, cells, pt[1], id) + lookup<S>(in, cells, pt[2], id);
-        s6 += lookup<S>(in, cells, pt[3], id);
-        s6 += lookup<S>(in, cells, pt[4], id);
-        s6 += lookup<S>(in, cells, pt[5], id);
-        s6 += lookup<S>(in, cells, pt[6], id);
-        vc[t] = v;
-        lapk[t] = (s6 - 6.0f * v) * P.inv_dx2;
-    }
-
-    const bool has_liq = n > 0 && ids[0] == LIQ;
+    const int n = A.n;
+    const bool has_liq = n > 0 && A.ids[0] == LIQ;
     const bool has_solid = n > (has_liq ? 1 : 0);
     float lap_sl[AMAX], b_sl[AMAX];
     float w_sl = P.w0;
-    for (int t = 0; t < n; ++t) {
-        lap_sl[t] = 0.0f;
-        b_sl[t] = 1.0f;
-    }
+    lap_sl[0] = 0.0f;
+    b_sl[0] = 1.0f;
     if (has_liq && has_solid) {
         if (HEAVY && P.use_aniso) {
-            const int pl[7] = {l, lp, lm, l, l, l, l};
-            const int pm[7] = {m, m, m, mp, mm, m, m};
-            const int pk[7] = {k, k, k, k, k, kp, km};
+            // liquid on the 25-point stencil (offsets with |dx|+|dy|+|dz| <= 2)
+            const int lpp = wrap_p(lp, P.nx), lmm = wrap_m(lm, P.nx);
+            const int mpp = wrap_p(mp, P.ny), mmm = wrap_m(mm, P.ny);
+            const int kpp = clamp_p(kp, P.nz), kmm = clamp_m(km, P.nz);
+            const float Lxpyp = liquid32(in, cidx(P, lp, mp, k)), Lxpym = liquid32(in, cidx(P, lp, mm, k));
+            const float Lxmyp = liquid32(in, cidx(P, lm, mp, k)), Lxmym = liquid32(in, cidx(P, lm, mm, k));
+            const float Lxpzp = liquid32(in, cidx(P, lp, m, kp)), Lxpzm = liquid32(in, cidx(P, lp, m, km));
+            const float Lxmzp = liquid32(in, cidx(P, lm, m, kp)), Lxmzm = liquid32(in, cidx(P, lm, m, km));
+            const float Lypzp = liquid32(in, cidx(P, l, mp, kp)), Lypzm = liquid32(in, cidx(P, l, mp, km));
+            const float Lymzp = liquid32(in, cidx(P, l, mm, kp)), Lymzm = liquid32(in, cidx(P, l, mm, km));
+            const float Lx2p = liquid32(in, cidx(P, lpp, m, k)), Lx2m = liquid32(in, cidx(P, lmm, m, k));
+            const float Ly2p = liquid32(in, cidx(P, l, mpp, k)), Ly2m = liquid32(in, cidx(P, l, mmm, k));
+            const float Lz2p = liquid32(in, cidx(P, l, m, kpp)), Lz2m = liquid32(in, cidx(P, l, m, kmm));
+            const float *vL = A.vL;
+            const float g2 = P.inv_2dx;
             float3 G[7];
-#pragma unroll
-            for (int p = 0; p < 7; ++p) G[p] = grad_liquid(in, P, pl[p], pm[p], pk[p]);
-            const float Lc = vc[0];
-            float Lp[7];
-#pragma unroll
-            for (int p = 1; p < 7; ++p) Lp[p] = liquid_at(in, cells, pt[p]);
-            // second derivatives of the liquid at the cell (d2_phi_xyz :207-248)
-            float pxx = 0.f, pyy = 0.f, pzz = 0.f, pxy = 0.f, pxz = 0.f, pyz = 0.f;
-            if (P.use_torque) {
-                pxx = (Lp[1] - 2.0f * Lc + Lp[2]) * P.inv_dx2;
-                pyy = (Lp[3] - 2.0f * Lc + Lp[4]) * P.inv_dx2;
-                pzz = (Lp[5] - 2.0f * Lc + Lp[6]) * P.inv_dx2;
-                const float qq = 0.25f * P.inv_dx2;
-                pxy = (liquid_at(in, cells, cell_of(P, lp, mp, k)) - liquid_at(in, cells, cell_of(P, lp, mm, k)) -
-                       liquid_at(in, cells, cell_of(P, lm, mp, k)) + liquid_at(in, cells, cell_of(P, lm, mm, k))) * qq;
-                pxz = (liquid_at(in, cells, cell_of(P, lp, m, kp)) - liquid_at(in, cells, cell_of(P, lp, m, km)) -
-                       liquid_at(in, cells, cell_of(P, lm, m, kp)) + liquid_at(in, cells, cell_of(P, lm, m, km))) * qq;
-                pyz = (liquid_at(in, cells, cell_of(P, l, mp, kp)) - liquid_at(in, cells, cell_of(P, l, mp, km)) -
-                       liquid_at(in, cells, cell_of(P, l, mm, kp)) + liquid_at(in, cells, cell_of(P, l, mm, km))) * qq;
-            }
-            for (int t = 1; t < n; ++t) {
-                const int g = ids[t];
-                const float *u = n111 + (size_t)g * 24;
-                Facet F[7];
-#pragma unroll
-                for (int p = 0; p < 7; ++p) F[p] = facet(G[p], u, P.g2_floor);
-                // div(eps^2 grad phi_L) with face-averaged eps^2 (aniso_term1_solid_3d :149-204)
-                float e2[7];
-#pragma unroll
-                for (int p = 0; p < 7; ++p) {
-                    const float e = P.eps0 * calc_a(P, F[p].cabs);
-                    e2[p] = e * e;
-                }
-                const float h = P.inv_2dx * P.inv_dx;
-                float lap_val = ((e2[0] + e2[1]) * (Lp[1] - Lc) - (e2[0] + e2[2]) * (Lc - Lp[2])) * h +
-                                ((e2[0] + e2[3]) * (Lp[3] - Lc) - (e2[0] + e2[4]) * (Lc - Lp[4])) * h +
-                                ((e2[0] + e2[5]) * (Lp[5] - Lc) - (e2[0] + e2[6]) * (Lc - Lp[6])) * h;
-                // torque (torque_A11_3d :386-441)
-                if (P.use_torque && F[0].valid) {
-                    const float3 g0 = G[0];
-                    const float q = F[0].q;
-                    const float qx = 2.0f * (g0.x * pxx + g0.y * pxy + g0.z * pxz);
-                    const float qy = 2.0f * (g0.x * pxy + g0.y * pyy + g0.z * pyz);
-                    const float qz = 2.0f * (g0.x * pxz + g0.y * pyz + g0.z * pzz);
-                    const float4 d0 = da_dgrad(P, g0, F[0]);
-                    const float ig = rsqrtf(q), ig3 = ig * ig * ig;
-                    const float ud = g0.x * F[0].nx + g0.y * F[0].ny + g0.z * F[0].nz;
-                    const float dcx = F[0].nx * ig - ud * g0.x * ig3;
-                    const float dcy = F[0].ny * ig - ud * g0.y * ig3;
-                    const float dcz = F[0].nz * ig - ud * g0.z * ig3;
-                    const float cxx = dcx * pxx + dcy * pxy + dcz * pxz;
-                    const float cyy = dcx * pxy + dcy * pyy + dcz * pyz;
-                    const float czz = dcx * pxz + dcy * pyz + dcz * pzz;
-                    const float cs = F[0].cs, cs2 = cs * cs;
-                    const float coef = P.mu_da * (cs / sqrtf(cs2 + P.pp) - P.tan_a0 * (cs / sqrtf(fmaxf(1.0f - cs2, 0.0f) + P.pp)));
-                    // A13_divergence_3d (:344-383)
-                    const float ddx = (da_dgrad(P, G[1], F[1]).y - da_dgrad(P, G[2], F[2]).y) * P.half_over_dx;
-                    const float ddy = (da_dgrad(P, G[3], F[3]).z - da_dgrad(P, G[4], F[4]).z) * P.half_over_dx;
-                    const float ddz = (da_dgrad(P, G[5], F[5]).w - da_dgrad(P, G[6], F[6]).w) * P.half_over_dx;
-                    const float a = d0.x;
-                    const float Ex = coef * cxx * d0.y * q + a * ddx * q + a * d0.y * qx;
-                    const float Ey = coef * cyy * d0.z * q + a * ddy * q + a * d0.z * qy;
-                    const float Ez = coef * czz * d0.w * q + a * ddz * q + a * d0.w * qz;
-                    lap_val += P.eps0sq * (Ex + Ey + Ez);
-                }
-                lap_sl[t] = lap_val;
-                b_sl[t] = calc_b(P, F[0].cabs);
-            }
-            // dominant solid and anisotropic solid-liquid potential (:579-595)
-            int ts = -1;
-            float maxv = -1.0f;
+            G[0] = make_float3((vL[1] - vL[2]) * g2, (vL[3] - vL[4]) * g2, (vL[5] - vL[6]) * g2);
+            G[1] = make_float3((Lx2p - vL[0]) * g2, (Lxpyp - Lxpym) * g2, (Lxpzp - Lxpzm) * g2);
+            G[2] = make_float3((vL[0] - Lx2m) * g2, (Lxmyp - Lxmym) * g2, (Lxmzp - Lxmzm) * g2);
+            G[3] = make_float3((Lxpyp - Lxmyp) * g2, (Ly2p - vL[0]) * g2, (Lypzp - Lypzm) * g2);
+            G[4] = make_float3((Lxpym - Lxmym) * g2, (vL[0] - Ly2m) * g2, (Lymzp - Lymzm) * g2);
+            // z neighbours sit on the clamped rows: at the top/bottom row the
+            // neighbour is the cell itself
+            G[5] = (kp == k) ? G[0] : make_float3((Lxpzp - Lxmzp) * g2, (Lypzp - Lymzp) * g2, (Lz2p - vL[0]) * g2);
+            G[6] = (km == k) ? G[0] : make_float3((Lxpzm - Lxmzm) * g2, (Lypzm - Lymzm) * g2, (vL[0] - Lz2m) * g2);
+            if (kp == k) G[5].z = (vL[5] - vL[6]) * g2;
+            if (km == k) G[6].z = (vL[5] - vL[6]) * g2;
+            float h2[6];
+            const float qq = 0.25f * P.inv_dx2;
+            h2[0] = (vL[1] - 2.0f * vL[0] + vL[2]) * P.inv_dx2;
+            h2[1] = (vL[3] - 2.0f * vL[0] + vL[4]) * P.inv_dx2;
+            h2[2] = (vL[5] - 2.0f * vL[0] + vL[6]) * P.inv_dx2;
+            h2[3] = (Lxpyp - Lxpym - Lxmyp + Lxmym) * qq;
+            h2[4] = (Lxpzp - Lxpzm - Lxmzp + Lxmzm) * qq;
+            h2[5] = (Lypzp - Lypzm - Lymzp + Lymzm) * qq;
             for (int t = 1; t < n; ++t)
-                if (vc[t] > maxv) { maxv = vc[t]; ts = t; }
-            if (ts > 0) {
-                const int g = ids[ts];
-                float3 gs;
-                gs.x = (lookup<S>(in, cells, pt[1], g) - lookup<S>(in, cells, pt[2], g)) * P.inv_2dx;
-                gs.y = (lookup<S>(in, cells, pt[3], g) - lookup<S>(in, cells, pt[4], g)) * P.inv_2dx;
-                gs.z = (lookup<S>(in, cells, pt[5], g) - lookup<S>(in, cells, pt[6], g)) * P.inv_2dx;
-                const Facet fs = facet(gs, n111 + (size_t)g * 24, P.g2_floor);
+                interface_terms(P, G, A.vL, h2, M.n111 + (size_t)A.ids[t] * 24, P.use_torque != 0, lap_sl[t], b_sl[t]);
+            if (A.ts > 0) {
+                const Facet fs = facet(A.gs, M.n111 + (size_t)A.ids[A.ts] * 24, P.g2_floor);
                 const float al = calc_a(P, fs.cabs);
                 w_sl = P.w0 * (al * al);
             }
         } else {
             // isotropic branch of the switchable kernel (:729-731)
-            for (int t = 1; t < n; ++t) lap_sl[t] = P.eps0sq * lapk[0];
+            for (int t = 1; t < n; ++t) {
+                lap_sl[t] = P.eps0sq * A.lap[0];
+                b_sl[t] = 1.0f;
+            }
+        }
+    } else {
+        for (int t = 1; t < n; ++t) {
+            lap_sl[t] = 0.0f;
+            b_sl[t] = 1.0f;
         }
     }
 
-    // pair sums (:600-661)
+    // Pair sums (:600-661) in O(n^2): for a pair (i, j) the t3 sum of the
+    // reference splits into W_i - W_j (potential) plus either the
+    // solid-liquid term of lap_sl or (A_i - A_j)/2 (gradient energy).
+    const int N = P.N;
+    float W[AMAX], Ag[AMAX];
+    for (int t1 = 0; t1 < n; ++t1) {
+        const int i = A.ids[t1];
+        float w = 0.0f, a = 0.0f;
+        for (int t3 = 0; t3 < n; ++t3) {
+            const int q = A.ids[t3];
+            const float wik = (q == LIQ && i != LIQ) ? w_sl : __ldg(M.wij + i * N + q);
+            w += wik * A.vc[t3];
+            a += __ldg(M.a2ij + i * N + q) * A.lap[t3];
+        }
+        W[t1] = w;
+        Ag[t1] = a;
+    }
     const float dT = (float)(M.T0z[k] - P.Tmc);
     const float inv_n = 1.0f / (float)(n > 0 ? n : 1);
-    const int N = P.N;
     float outv[AMAX];
     for (int t1 = 0; t1 < n; ++t1) {
-        const int i = ids[t1];
+        const int i = A.ids[t1];
         float dpi = 0.0f;
         for (int t2 = 0; t2 < n; ++t2) {
-            const int j = ids[t2];
-            if (i == j) continue;
+            if (t2 == t1) continue;
+            const int j = A.ids[t2];
             const bool sl = (i != LIQ && j == LIQ), ls = (i == LIQ && j != LIQ);
+            const float T = sl ? 0.5f * lap_sl[t1] : (ls ? -0.5f * lap_sl[t2] : 0.5f * (Ag[t1] - Ag[t2]));
+            const float ppp = (W[t1] - W[t2]) + T;
             const float df = sl ? -P.Sf * dT : (ls ? P.Sf * dT : 0.0f);
-            float ppp = 0.0f;
-            for (int t3 = 0; t3 < n; ++t3) {
-                const int q = ids[t3];
-                float wik = __ldg(wij + i * N + q), wjk = __ldg(wij + j * N + q);
-                if (q == LIQ) {
-                    if (i != LIQ) wik = w_sl;
-                    if (j != LIQ) wjk = w_sl;
-                }
-                float term2 = 0.0f;
-                if (sl) {
-                    if (q == i) term2 = 0.5f * lap_sl[t1];
-                } else if (ls) {
-                    if (q == j) term2 = -0.5f * lap_sl[t2];
-                } else {
-                    term2 = 0.5f * (__ldg(a2ij + i * N + q) - __ldg(a2ij + j * N + q)) * lapk[t3];
-                }
-                ppp += (wik - wjk) * vc[t3] + term2;
-            }
-            const float tf = FORCE_PREF * sqrtf(fmaxf(vc[t1] * vc[t2], 0.0f)) * df;
-            float me = __ldg(mij + i * N + j);
+            const float tf = FORCE_PREF * sqrtf(fmaxf(A.vc[t1] * A.vc[t2], 0.0f)) * df;
+            float me = __ldg(M.mij + i * N + j);
             if (sl) me *= b_sl[t1];
             else if (ls) me *= b_sl[t2];
             dpi -= 2.0f * me * inv_n * (ppp - tf);
         }
-        outv[t1] = fminf(fmaxf(vc[t1] + P.dt * dpi, 0.0f), 1.0f);
+        outv[t1] = fminf(fmaxf(A.vc[t1] + P.dt * dpi, 0.0f), 1.0f);
     }
 
     // renormalise with a compensated (TwoSum) float accumulation (:663-680)
     float sh = 0.0f, sl_ = 0.0f;
     for (int t = 0; t < n; ++t) {
         const float a = sh, b = outv[t];
-        const float s = a + b;
-        const float bb = s - a;
-        sl_ += (a - (s - bb)) + (b - bb);
-        sh = s;
+        const float s2 = a + b;
+        const float bb = s2 - a;
+        sl_ += (a - (s2 - bb)) + (b - bb);
+        sh = s2;
     }
-    const float stot = sh + sl_;
     int cnt_out = 0;
     bool sovf = false;
-    if (stot > 1e-20f) {
+    if (sh + sl_ > 1e-20f) {
         float inv = 1.0f / sh;
         inv = inv - inv * inv * sl_;
         for (int t = 0; t < n; ++t) {
             const float v = outv[t] * inv;
             if (v > 0.0f) {
                 if (cnt_out < S) {
-                    out.idx[cnt_out * cells + c] = (uint16_t)ids[t];
-                    out.val[cnt_out * cells + c] = v;
+                    out.idx[(uint32_t)cnt_out * cells + c] = (uint16_t)A.ids[t];
+                    out.val[(uint32_t)cnt_out * cells + c] = v;
                     ++cnt_out;
                 } else {
                     sovf = true;
@@ -418,10 +476,10 @@ __device__ __forceinline__ void process_cell(const In &in, const Out &out, const
         out.val[c] = 1.0f;
         cnt_out = 1;
         for (int t = 0; t < n; ++t) {
-            if (ids[t] == LIQ || !(outv[t] > 0.0f)) continue;
+            if (A.ids[t] == LIQ || !(outv[t] > 0.0f)) continue;
             if (cnt_out < S) {
-                out.idx[cnt_out * cells + c] = (uint16_t)ids[t];
-                out.val[cnt_out * cells + c] = outv[t];
+                out.idx[(uint32_t)cnt_out * cells + c] = (uint16_t)A.ids[t];
+                out.val[(uint32_t)cnt_out * cells + c] = outv[t];
                 ++cnt_out;
             } else {
                 sovf = true;
@@ -450,9 +508,9 @@ __global__ void __launch_bounds__(256) sweep_kernel(In in, Out out, Mats M, Para
     if (l >= P.nx || m >= P.ny || k >= P.nz) return;
     const int lp = wrap_p(l, P.nx), lm = wrap_m(l, P.nx), mp = wrap_p(m, P.ny), mm = wrap_m(m, P.ny);
     const int kp = clamp_p(k, P.nz), km = clamp_m(k, P.nz);
-    const int64_t c = cell_of(P, l, m, k);
-    const int64_t nb[6] = {cell_of(P, lp, m, k), cell_of(P, lm, m, k), cell_of(P, l, mp, k),
-                           cell_of(P, l, mm, k), cell_of(P, l, m, kp), cell_of(P, l, m, km)};
+    const uint32_t c = cidx(P, l, m, k);
+    const uint32_t nb[6] = {cidx(P, lp, m, k), cidx(P, lm, m, k), cidx(P, l, mp, k),
+                            cidx(P, l, mm, k), cidx(P, l, m, kp), cidx(P, l, m, km)};
     const int c0 = __ldg(in.cnt + c);
     const int i0 = __ldg(in.idx + c);
     bool uniform = (c0 == 1);
@@ -481,7 +539,7 @@ __global__ void __launch_bounds__(256) sweep_kernel(In in, Out out, Mats M, Para
         uint32_t base = 0;
         if (lane == leader) base = atomicAdd(Q.count + parity, (uint32_t)__popc(bm));
         base = __shfl_sync(am, base, leader);
-        if (push) Q.items[base + __popc(bm & ((1u << lane) - 1u))] = (uint32_t)c;
+        if (push) Q.items[base + __popc(bm & ((1u << lane) - 1u))] = c;
     }
     if (push) return;
     process_cell<S, AMAX, false>(in, out, M, P, err, l, m, k);
@@ -490,8 +548,8 @@ __global__ void __launch_bounds__(256) sweep_kernel(In in, Out out, Mats M, Para
 // Kernel 2 of a step: the queued solid-liquid interface cells, one thread
 // per cell, all lanes of a warp on the same (heavy) path.
 template <int S, int AMAX>
-__global__ void __launch_bounds__(128) interface_kernel(In in, Out out, Mats M, Params P, Queue Q, int parity,
-                                                        int32_t *__restrict__ err) {
+__global__ void __launch_bounds__(128, 4) interface_kernel(In in, Out out, Mats M, Params P, Queue Q, int parity,
+                                                           int32_t *__restrict__ err) {
     const uint32_t n = *(volatile uint32_t *)(Q.count + parity);
     const uint32_t plane = (uint32_t)P.nx * (uint32_t)P.ny;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -713,6 +771,23 @@ extern "C" int mpf3d_compact_step(const uint8_t *cnt, const uint16_t *idx, const
     P.Tmc = Tm_plus_cool;
     P.use_aniso = enable_anisotropy != 0;
     P.use_torque = enable_anisotropy != 0 && enable_torque != 0;
+    P.cells32 = (uint32_t)P.cells;
+    {
+        // a(0) and b(0): the values for a gradient below g2_floor
+        const double pp = v[MPF3D_S_P_ROUND] * v[MPF3D_S_P_ROUND];
+        const double a_flat = v[MPF3D_S_MU_A] * (1.0 + v[MPF3D_S_DELTA_A] * (sqrt(pp) + tan(v[MPF3D_S_A0]) * sqrt(1.0 + pp)));
+        const double e = v[MPF3D_S_EPS0_SL] * a_flat;
+        P.e2_flat = (float)(e * e);
+        const double th = acos(0.0), thc = v[MPF3D_S_THETA_C_RAD];
+        double b = 1.0;
+        if (th < thc) {
+            double y = 0.5 * 3.14159265358979323846 * (th / thc);
+            y = fmin(fmax(y, 1e-6), 0.5 * 3.14159265358979323846 - 1e-6);
+            const double t = tan(y);
+            b = v[MPF3D_S_KSI] + (1.0 - v[MPF3D_S_KSI]) * t * tanh(1.0 / t);
+        }
+        P.b_flat = (float)b;
+    }
     In in{cnt, idx, val};
     Out out{cnt_out, idx_out, val_out};
     Mats M{T0z, wij, a2ij, mij, n111};
