@@ -112,17 +112,20 @@ int mpf3d_compact_active_count(const uint8_t *cnt, const uint16_t *idx, int slot
  * (16, 32); more active phases than amax, or more positive phases than
  * slots, leave the cell unchanged and set MPF3D_DEV_SLOT_OVERFLOW.
  * a2ij = aij*aij elementwise (float32).  T0z: float64 [nz].
- * Scratch: work_items uint32[cells] (the solid-liquid interface cells of the
- * step, handed from the sweep kernel to the interface kernel) and
- * work_count uint32[2], zeroed once before the first step; `parity`
- * alternates 0/1 on consecutive steps so no reset is needed in between.
- * Cells must number fewer than 2^31. */
+ * symmetric_normals != 0 asserts that every grain's n111 rows 4..7 are the
+ * exact negatives of rows 3..0 (true for the rotated (+-1,+-1,+-1)/sqrt(3)
+ * set of src/orientation_utils.py:182-212), which halves the facet search.
+ * Scratch: work_items uint32[cells] (cells handed from the sweep kernel to
+ * the general and interface kernels of the step) and work_count uint32[4],
+ * zeroed once before the first step; `parity` alternates 0/1 on consecutive
+ * steps so no reset is needed in between.  Cells must number fewer than 2^31. */
 int mpf3d_compact_step(const uint8_t *cnt, const uint16_t *idx, const float *val, uint8_t *cnt_out,
                        uint16_t *idx_out, float *val_out, int slots, int amax, const double *T0z,
                        double Tm_plus_cool, const float *wij, const float *a2ij, const float *mij,
                        const float *n111, int N, int nx, int ny, int nz, const mpf3d_scalars *scalars,
-                       int enable_anisotropy, int enable_torque, uint32_t *work_items,
-                       uint32_t *work_count, int parity, int32_t *err, void *stream);
+                       int enable_anisotropy, int enable_torque, int symmetric_normals,
+                       uint32_t *work_items, uint32_t *work_count, int parity, int32_t *err,
+                       void *stream);
 
 /* library version, for the binding's load check */
 int mpf3d_version(void);

@@ -39,6 +39,7 @@ struct Params {
     float eps0, eps0sq, w0, mu_a, delta_a, mu_da, pp, tan_a0, g2_floor, ksi, theta_c, Sf;
     double Tmc;  // T_melt + accumulated cooling (float64)
     int use_aniso, use_torque;
+    int sym_normals;  // every grain's n111 rows 4..7 are -(rows 3..0)
 };
 
 struct In {
@@ -99,7 +100,12 @@ struct Facet {
     float cabs, cs, nx, ny, nz, q;
 };
 
-__device__ __forceinline__ Facet facet(float3 g, const float *__restrict__ u, float g2_floor) {
+// When the 8 normals are 4 exact antipodal pairs with one member of each
+// pair among the first four (true for the rotated (+-1,+-1,+-1)/sqrt(3) set
+// in the reference's order; checked on the host), |cos| ties exactly within
+// a pair and the first-maximum search over 8 equals the search over 4.
+template <int NT = 8>
+__device__ __forceinline__ Facet facet_n(float3 g, const float *__restrict__ u, float g2_floor) {
     Facet f;
     f.q = g.x * g.x + g.y * g.y + g.z * g.z;
     f.valid = !(f.q < g2_floor);
@@ -108,7 +114,7 @@ __device__ __forceinline__ Facet facet(float3 g, const float *__restrict__ u, fl
     float ig = rsqrtf(f.q);
     float gx = g.x * ig, gy = g.y * ig, gz = g.z * ig;
 #pragma unroll
-    for (int t = 0; t < 8; ++t) {
+    for (int t = 0; t < NT; ++t) {
         float ux = __ldg(u + 3 * t), uy = __ldg(u + 3 * t + 1), uz = __ldg(u + 3 * t + 2);
         float d = gx * ux + gy * uy + gz * uz;
         float a = fabsf(d);
@@ -119,6 +125,10 @@ __device__ __forceinline__ Facet facet(float3 g, const float *__restrict__ u, fl
     f.cabs = fminf(f.cabs, 1.0f);
     f.cs = fminf(fmaxf(f.cs, -1.0f), 1.0f);
     return f;
+}
+
+__device__ __forceinline__ Facet facet(float3 g, const float *__restrict__ u, float g2_floor, bool sym) {
+    return sym ? facet_n<4>(g, u, g2_floor) : facet_n<8>(g, u, g2_floor);
 }
 
 // a(theta) (calc_a_from_cos :24-30)
@@ -156,10 +166,11 @@ __device__ __forceinline__ float4 da_dgrad(const Params &P, float3 g, const Face
                        coef * (f.nz * ig - ud * g.z * ig3));
 }
 
-// Work list of solid-liquid interface cells for the second kernel of a
-// step (scratch memory owned by the caller): items[] holds x-fastest cell
-// indices, count[2] two counters used on alternate steps so that no memset
-// is needed between steps.
+// Work lists of a step (scratch memory owned by the caller): items[cells]
+// holds x-fastest cell indices -- cells needing the general update from the
+// front, solid-liquid interface cells from the back; count[4] holds the two
+// list lengths for even and odd steps (count[2*parity + 0/1]), so the sweep
+// of one step can clear the other parity's counters without a memset.
 struct Queue {
     uint32_t *__restrict__ items;
     uint32_t *__restrict__ count;
@@ -261,7 +272,7 @@ __device__ __forceinline__ void interface_terms(const Params &P, const float3 (&
     bool any = false;
 #pragma unroll
     for (int p = 0; p < 7; ++p) {
-        F[p] = facet(G[p], u, P.g2_floor);
+        F[p] = facet(G[p], u, P.g2_floor, P.sym_normals != 0);
         any = any || F[p].valid;
     }
     const float Lc = vL[0];
@@ -387,7 +398,7 @@ __device__ __forceinline__ void process_cell(const In &in, const Out &out, const
             for (int t = 1; t < n; ++t)
                 interface_terms(P, G, A.vL, h2, M.n111 + (size_t)A.ids[t] * 24, P.use_torque != 0, lap_sl[t], b_sl[t]);
             if (A.ts > 0) {
-                const Facet fs = facet(A.gs, M.n111 + (size_t)A.ids[A.ts] * 24, P.g2_floor);
+                const Facet fs = facet(A.gs, M.n111 + (size_t)A.ids[A.ts] * 24, P.g2_floor, P.sym_normals != 0);
                 const float al = calc_a(P, fs.cabs);
                 w_sl = P.w0 * (al * al);
             }
@@ -492,19 +503,35 @@ __device__ __forceinline__ void process_cell(const In &in, const Out &out, const
 
 // Kernel 1 of a step: every cell.  Uniform neighbourhoods (the cell and its
 // 6 neighbours hold one and the same phase: active list of one phase, empty
-// pair sums, renormalised fraction exactly 1) are written directly;
-// neighbourhoods holding both liquid and a solid are queued for kernel 2
-// when anisotropy is on; all others (grain boundaries, junctions without
-// liquid, the isotropic model) are updated here.
+// pair sums, renormalised fraction exactly 1) are written directly; every
+// other cell is appended to a work list -- solid-liquid interface cells
+// (liquid and a solid in the neighbourhood, anisotropy on) to the back,
+// the rest (grain boundaries, junctions without liquid, the isotropic model)
+// to the front -- so that the general update runs with converged warps.
+__device__ __forceinline__ void push(const Queue &Q, int parity, bool want, bool back, uint32_t cells, uint32_t c) {
+    const unsigned am = __activemask();
+    const unsigned bm = __ballot_sync(am, want);
+    if (!bm) return;
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(bm) - 1;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(Q.count + 2 * parity + (back ? 1 : 0), (uint32_t)__popc(bm));
+    base = __shfl_sync(am, base, leader);
+    if (want) {
+        const uint32_t pos = base + __popc(bm & ((1u << lane) - 1u));
+        Q.items[back ? cells - 1u - pos : pos] = c;
+    }
+}
+
 template <int S, int AMAX>
 __global__ void __launch_bounds__(256) sweep_kernel(In in, Out out, Mats M, Params P, Queue Q, int parity,
                                                     int32_t *__restrict__ err) {
     const int l = blockIdx.x * blockDim.x + threadIdx.x;
     const int m = blockIdx.y * blockDim.y + threadIdx.y;
     const int k = blockIdx.z * blockDim.z + threadIdx.z;
-    if (blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.x == 0 && threadIdx.y == 0 &&
+    if (blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.x < 2 && threadIdx.y == 0 &&
         threadIdx.z == 0)
-        Q.count[parity ^ 1] = 0;  // kernel 2 of the previous step has finished with it
+        Q.count[2 * (parity ^ 1) + threadIdx.x] = 0;  // the previous step's kernels are done with them
     if (l >= P.nx || m >= P.ny || k >= P.nz) return;
     const int lp = wrap_p(l, P.nx), lm = wrap_m(l, P.nx), mp = wrap_p(m, P.ny), mm = wrap_m(m, P.ny);
     const int kp = clamp_p(k, P.nz), km = clamp_m(k, P.nz);
@@ -530,30 +557,37 @@ __global__ void __launch_bounds__(256) sweep_kernel(In in, Out out, Mats M, Para
         out.val[c] = 1.0f;
         return;
     }
-    const bool push = liq && sol && P.use_aniso;
-    const unsigned am = __activemask();
-    const unsigned bm = __ballot_sync(am, push);
-    if (bm) {
-        const int lane = threadIdx.x & 31;
-        const int leader = __ffs(bm) - 1;
-        uint32_t base = 0;
-        if (lane == leader) base = atomicAdd(Q.count + parity, (uint32_t)__popc(bm));
-        base = __shfl_sync(am, base, leader);
-        if (push) Q.items[base + __popc(bm & ((1u << lane) - 1u))] = c;
-    }
-    if (push) return;
-    process_cell<S, AMAX, false>(in, out, M, P, err, l, m, k);
+    const bool heavy = liq && sol && P.use_aniso;
+    push(Q, parity, heavy, true, P.cells32, c);
+    push(Q, parity, !heavy, false, P.cells32, c);
 }
 
-// Kernel 2 of a step: the queued solid-liquid interface cells, one thread
+// Kernel 2 of a step: the cells queued for the general update, one thread
+// per cell.
+template <int S, int AMAX>
+__global__ void __launch_bounds__(256) general_kernel(In in, Out out, Mats M, Params P, Queue Q, int parity,
+                                                     int32_t *__restrict__ err) {
+    const uint32_t n = *(volatile uint32_t *)(Q.count + 2 * parity);
+    const uint32_t plane = (uint32_t)P.nx * (uint32_t)P.ny;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t c = Q.items[i];
+        const int k = (int)(c / plane);
+        const uint32_t r = c - (uint32_t)k * plane;
+        const int m = (int)(r / (uint32_t)P.nx);
+        const int l = (int)(r - (uint32_t)m * (uint32_t)P.nx);
+        process_cell<S, AMAX, false>(in, out, M, P, err, l, m, k);
+    }
+}
+
+// Kernel 3 of a step: the queued solid-liquid interface cells, one thread
 // per cell, all lanes of a warp on the same (heavy) path.
 template <int S, int AMAX>
 __global__ void __launch_bounds__(128, 4) interface_kernel(In in, Out out, Mats M, Params P, Queue Q, int parity,
                                                            int32_t *__restrict__ err) {
-    const uint32_t n = *(volatile uint32_t *)(Q.count + parity);
+    const uint32_t n = *(volatile uint32_t *)(Q.count + 2 * parity + 1);
     const uint32_t plane = (uint32_t)P.nx * (uint32_t)P.ny;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const uint32_t c = Q.items[i];
+        const uint32_t c = Q.items[P.cells32 - 1u - i];
         const int k = (int)(c / plane);
         const uint32_t r = c - (uint32_t)k * plane;
         const int m = (int)(r / (uint32_t)P.nx);
@@ -668,12 +702,11 @@ void launch_step(const In &in, const Out &out, const Mats &M, const Params &P, c
     dim3 blk(32, 4, 2);
     dim3 grd((P.nx + 31) / 32, (P.ny + 3) / 4, (P.nz + 1) / 2);
     sweep_kernel<S, AMAX><<<grd, blk, 0, s>>>(in, out, M, P, Q, parity, err);
-    if (P.use_aniso) {
-        int dev = 0, sms = 148;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        interface_kernel<S, AMAX><<<sms * 8, 128, 0, s>>>(in, out, M, P, Q, parity, err);
-    }
+    int dev = 0, sms = 148;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    general_kernel<S, AMAX><<<sms * 8, 256, 0, s>>>(in, out, M, P, Q, parity, err);
+    if (P.use_aniso) interface_kernel<S, AMAX><<<sms * 8, 128, 0, s>>>(in, out, M, P, Q, parity, err);
 }
 
 }  // namespace
@@ -738,8 +771,9 @@ extern "C" int mpf3d_compact_step(const uint8_t *cnt, const uint16_t *idx, const
                                   uint16_t *idx_out, float *val_out, int slots, int amax, const double *T0z,
                                   double Tm_plus_cool, const float *wij, const float *a2ij, const float *mij,
                                   const float *n111, int N, int nx, int ny, int nz, const mpf3d_scalars *sc,
-                                  int enable_anisotropy, int enable_torque, uint32_t *work_items,
-                                  uint32_t *work_count, int parity, int32_t *err, void *stream) {
+                                  int enable_anisotropy, int enable_torque, int symmetric_normals,
+                                  uint32_t *work_items, uint32_t *work_count, int parity, int32_t *err,
+                                  void *stream) {
     if (!cnt || !idx || !val || !cnt_out || !idx_out || !val_out || !T0z || !wij || !a2ij || !mij || !n111 || !sc ||
         !err || !work_items || !work_count)
         return MPF3D_ERR_ARG;
@@ -772,6 +806,7 @@ extern "C" int mpf3d_compact_step(const uint8_t *cnt, const uint16_t *idx, const
     P.use_aniso = enable_anisotropy != 0;
     P.use_torque = enable_anisotropy != 0 && enable_torque != 0;
     P.cells32 = (uint32_t)P.cells;
+    P.sym_normals = symmetric_normals != 0;
     {
         // a(0) and b(0): the values for a gradient below g2_floor
         const double pp = v[MPF3D_S_P_ROUND] * v[MPF3D_S_P_ROUND];

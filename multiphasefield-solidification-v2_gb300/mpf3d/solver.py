@@ -96,7 +96,9 @@ class CompactSolver:
         self.err = torch.zeros(1, dtype=torch.int32, device=self.device)
         # scratch of the step: interface work list and its two counters
         self.work_items = torch.empty(self.cells, dtype=torch.int32, device=self.device)
-        self.work_count = torch.zeros(2, dtype=torch.int32, device=self.device)
+        self.work_count = torch.zeros(4, dtype=torch.int32, device=self.device)
+        n111_np = np.asarray(n111, np.float32)
+        self.symmetric_normals = bool(np.array_equal(n111_np[:, 4:8], -n111_np[:, [3, 2, 1, 0]]))
         self.buf = [self._alloc(), self._alloc()]
         self.cur = 0
         self.step_count = 0
@@ -134,7 +136,8 @@ class CompactSolver:
             dst[1].data_ptr(), dst[2].data_ptr(), self.slots, self.amax, self.T0z.data_ptr(), tmc,
             self.wij.data_ptr(), self.a2ij.data_ptr(), self.mij.data_ptr(), self.n111.data_ptr(),
             self.N, self.nx, self.ny, self.nz, ctypes.byref(self.scalars), int(self.anisotropy),
-            int(self.torque), self.work_items.data_ptr(), self.work_count.data_ptr(),
+            int(self.torque), int(self.symmetric_normals), self.work_items.data_ptr(),
+            self.work_count.data_ptr(),
             step_index & 1, self.err.data_ptr(), self._stream())
         _lib.check(rc, "compact_step")
         self.cur = 1 - self.cur
