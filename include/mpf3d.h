@@ -86,7 +86,12 @@ int mpf3d_dense_temp(void *temp, int temp_dtype, double cooling_rate, int rate_i
 
 /* ---- compact FP32 tier (fused step) -------------------------------------
  * State of one buffer (x fastest: cell = (k*ny + m)*nx + l):
- *   cnt uint8[cells], idx uint16[slots][cells] (ascending ids), val float[slots][cells]
+ *   head uint32[cells]        bits 0-6 number n of stored phases (phi > 0),
+ *                             bit 7 single value stored explicitly,
+ *                             bits 8-23 id of the smallest stored phase
+ *   idx  uint16[slots][cells] ids of stored phases 1..n-1, ascending (slot 0 unused)
+ *   val  float[slots][cells]  fractions of stored phases 0..n-1; a cell whose
+ *                             only stored phase is exactly 1 keeps no value
  * slots is 4, 8 or 16.  No reference counterpart for the layout: it replaces
  * the dense phi [N][nx][ny][nz] + mf/nf arrays of src/gpu_kernels_3d.py. */
 
@@ -94,15 +99,15 @@ int mpf3d_dense_temp(void *temp, int temp_dtype, double cooling_rate, int rate_i
  * entries set MPF3D_DEV_BAD_INPUT; more than `slots` positive phases in a
  * cell set MPF3D_DEV_SLOT_OVERFLOW. */
 int mpf3d_compact_from_dense(const void *phi, int phi_dtype, int N, int nx, int ny, int nz, int slots,
-                             uint8_t *cnt, uint16_t *idx, float *val, int32_t *err, void *stream);
+                             uint32_t *head, uint16_t *idx, float *val, int32_t *err, void *stream);
 
 /* compact state -> dense phi (every phase written, zeros included). */
-int mpf3d_compact_to_dense(const uint8_t *cnt, const uint16_t *idx, const float *val, int slots, int N,
+int mpf3d_compact_to_dense(const uint32_t *head, const uint16_t *idx, const float *val, int slots, int N,
                            int nx, int ny, int nz, void *phi, int phi_dtype, void *stream);
 
 /* nf of the reference's APT (kernel_update_nfmf_3d, src/gpu_kernels_3d.py:462-486)
  * computed from a compact state, dense z-fastest int32 output. */
-int mpf3d_compact_active_count(const uint8_t *cnt, const uint16_t *idx, int slots, int nx, int ny, int nz,
+int mpf3d_compact_active_count(const uint32_t *head, const uint16_t *idx, int slots, int nx, int ny, int nz,
                                int32_t *nf, void *stream);
 
 /* One fused time step in FP32: APT rebuild (src/gpu_kernels_3d.py:462-486),
@@ -119,7 +124,7 @@ int mpf3d_compact_active_count(const uint8_t *cnt, const uint16_t *idx, int slot
  * the general and interface kernels of the step) and work_count uint32[4],
  * zeroed once before the first step; `parity` alternates 0/1 on consecutive
  * steps so no reset is needed in between.  Cells must number fewer than 2^31. */
-int mpf3d_compact_step(const uint8_t *cnt, const uint16_t *idx, const float *val, uint8_t *cnt_out,
+int mpf3d_compact_step(const uint32_t *head, const uint16_t *idx, const float *val, uint32_t *head_out,
                        uint16_t *idx_out, float *val_out, int slots, int amax, const double *T0z,
                        double Tm_plus_cool, const float *wij, const float *a2ij, const float *mij,
                        const float *n111, int N, int nx, int ny, int nz, const mpf3d_scalars *scalars,

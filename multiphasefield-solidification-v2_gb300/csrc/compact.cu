@@ -10,9 +10,13 @@
 // State layout in HBM (x fastest, so a warp of 32 threads along x reads
 // 32 consecutive entries of each array and an interface -- normal to z --
 // keeps a warp convergent):
-//   cnt  uint8 [cells]            number of stored phases (phi > 0)
-//   idx  uint16[S][cells]         stored phase ids, ascending
-//   val  float [S][cells]         stored phase fractions
+//   head uint32[cells]     bits 0-6 number n of stored phases (phi > 0),
+//                          bit 7 "single value stored explicitly",
+//                          bits 8-23 id of the first (smallest) stored phase
+//   idx  uint16[S][cells]  ids of stored phases 1..n-1 (ascending; slot 0 unused)
+//   val  float [S][cells]  fractions of stored phases 0..n-1
+// A cell holding one phase at exactly 1 -- about nine cells in ten in a
+// directional-solidification run -- costs 4 bytes: its value is implicit.
 // Temperature is T0[z] - (accumulated cooling) with the accumulator in
 // float64 on the host; the per-cell sum-to-one uses a compensated float
 // pair (TwoSum), which keeps GB300's slow float64 pipe out of the loop.
@@ -43,15 +47,26 @@ struct Params {
 };
 
 struct In {
-    const uint8_t *__restrict__ cnt;
+    const uint32_t *__restrict__ head;
     const uint16_t *__restrict__ idx;
     const float *__restrict__ val;
 };
 struct Out {
-    uint8_t *__restrict__ cnt;
+    uint32_t *__restrict__ head;
     uint16_t *__restrict__ idx;
     float *__restrict__ val;
 };
+
+__device__ __forceinline__ int hcount(uint32_t h) { return (int)(h & 0x7Fu); }
+__device__ __forceinline__ bool hexplicit(uint32_t h) { return (h & 0x80u) != 0u; }
+__device__ __forceinline__ int hid0(uint32_t h) { return (int)(h >> 8); }
+__device__ __forceinline__ uint32_t mkhead(int id0, int n, bool expl) {
+    return ((uint32_t)id0 << 8) | (expl ? 0x80u : 0u) | (uint32_t)n;
+}
+// value of stored entry 0 of a cell with head h
+__device__ __forceinline__ float value0(const In &in, uint32_t h, uint32_t q) {
+    return (hcount(h) >= 2 || hexplicit(h)) ? __ldg(in.val + q) : 1.0f;
+}
 
 __device__ __forceinline__ int wrap_p(int l, int n) { return l < n - 1 ? l + 1 : 0; }
 __device__ __forceinline__ int wrap_m(int l, int n) { return l > 0 ? l - 1 : n - 1; }
@@ -60,36 +75,6 @@ __device__ __forceinline__ int clamp_m(int k, int n) { return k > 0 ? k - 1 : 0;
 
 __device__ __forceinline__ int64_t cell_of(const Params &P, int l, int m, int k) {
     return ((int64_t)k * P.ny + m) * P.nx + l;
-}
-
-// stored fraction of phase `id` at cell q (0 when not stored)
-template <int S>
-__device__ __forceinline__ float lookup(const In &in, int64_t cells, int64_t q, int id) {
-    int c = __ldg(in.cnt + q);
-    c = c < S ? c : S;
-    for (int s = 0; s < c; ++s) {
-        int v = __ldg(in.idx + s * cells + q);
-        if (v == id) return __ldg(in.val + s * cells + q);
-        if (v > id) break;
-    }
-    return 0.0f;
-}
-
-// liquid fraction at cell q: the liquid (id 0) sorts first when stored
-__device__ __forceinline__ float liquid_at(const In &in, int64_t cells, int64_t q) {
-    int c = __ldg(in.cnt + q);
-    if (c == 0 || __ldg(in.idx + q) != LIQ) return 0.0f;
-    return __ldg(in.val + q);
-}
-
-__device__ __forceinline__ float3 grad_liquid(const In &in, const Params &P, int l, int m, int k) {
-    int lp = wrap_p(l, P.nx), lm = wrap_m(l, P.nx), mp = wrap_p(m, P.ny), mm = wrap_m(m, P.ny);
-    int kp = clamp_p(k, P.nz), km = clamp_m(k, P.nz);
-    float3 g;
-    g.x = (liquid_at(in, P.cells, cell_of(P, lp, m, k)) - liquid_at(in, P.cells, cell_of(P, lm, m, k))) * P.inv_2dx;
-    g.y = (liquid_at(in, P.cells, cell_of(P, l, mp, k)) - liquid_at(in, P.cells, cell_of(P, l, mm, k))) * P.inv_2dx;
-    g.z = (liquid_at(in, P.cells, cell_of(P, l, m, kp)) - liquid_at(in, P.cells, cell_of(P, l, m, km))) * P.inv_2dx;
-    return g;
 }
 
 // max |cos| between a gradient and the grain's 8 rotated {111} normals, with
@@ -189,9 +174,9 @@ __device__ __forceinline__ uint32_t cidx(const Params &P, int l, int m, int k) {
 }
 
 __device__ __forceinline__ float liquid32(const In &in, uint32_t q) {
-    const int c = __ldg(in.cnt + q);
-    if (c == 0 || __ldg(in.idx + q) != LIQ) return 0.0f;
-    return __ldg(in.val + q);
+    const uint32_t h = __ldg(in.head + q);
+    if (hcount(h) == 0 || hid0(h) != LIQ) return 0.0f;
+    return value0(in, h, q);
 }
 
 // Active list of one cell: the ascending union of the stored lists of the
@@ -214,12 +199,14 @@ template <int S, int AMAX>
 __device__ __forceinline__ void gather(const In &in, const Params &P, const uint32_t (&pt)[7], Active<AMAX> &A) {
     const uint32_t cells = P.cells32;
     int cnt[7], pos[7], head[7];
+    uint32_t hw[7];
 #pragma unroll
     for (int p = 0; p < 7; ++p) {
-        const int c = __ldg(in.cnt + pt[p]);
+        hw[p] = __ldg(in.head + pt[p]);
+        const int c = hcount(hw[p]);
         cnt[p] = c < S ? c : S;
         pos[p] = 0;
-        head[p] = cnt[p] > 0 ? (int)__ldg(in.idx + pt[p]) : 0x7fffffff;
+        head[p] = cnt[p] > 0 ? hid0(hw[p]) : 0x7fffffff;
         A.vL[p] = 0.0f;
     }
     A.n = 0;
@@ -237,7 +224,7 @@ __device__ __forceinline__ void gather(const In &in, const Params &P, const uint
         for (int p = 0; p < 7; ++p) {
             v[p] = 0.0f;
             if (head[p] == id) {
-                v[p] = __ldg(in.val + (uint32_t)pos[p] * cells + pt[p]);
+                v[p] = pos[p] == 0 ? value0(in, hw[p], pt[p]) : __ldg(in.val + (uint32_t)pos[p] * cells + pt[p]);
                 ++pos[p];
                 head[p] = pos[p] < cnt[p] ? (int)__ldg(in.idx + (uint32_t)pos[p] * cells + pt[p]) : 0x7fffffff;
             }
@@ -265,7 +252,7 @@ __device__ __forceinline__ void gather(const In &in, const Params &P, const uint
 // a cell from the liquid gradient at the 7 points and the liquid's second
 // derivatives at the cell (aniso_term1_solid_3d :149-204, torque_A11_3d
 // :386-441, A13_divergence_3d :344-383, calc_b_from_cos :33-55).
-__device__ __forceinline__ void interface_terms(const Params &P, const float3 (&G)[7], const float (&vL)[7],
+__device__ __noinline__ void interface_terms(const Params &P, const float3 (&G)[7], const float (&vL)[7],
                                                 const float (&h2)[6], const float *__restrict__ u, bool torque,
                                                 float &lap_sl, float &b_sl) {
     Facet F[7];
@@ -343,8 +330,9 @@ __device__ __forceinline__ void process_cell(const In &in, const Out &out, const
         // leave the cell as it was and report; the host re-runs the step with
         // a wider template
         atomicOr(err, MPF3D_DEV_SLOT_OVERFLOW);
-        const int c0 = min((int)__ldg(in.cnt + c), S);
-        out.cnt[c] = (uint8_t)c0;
+        const uint32_t h0 = __ldg(in.head + c);
+        const int c0 = min(hcount(h0), S);
+        out.head[c] = h0;
         for (int s = 0; s < c0; ++s) {
             out.idx[(uint32_t)s * cells + c] = __ldg(in.idx + (uint32_t)s * cells + c);
             out.val[(uint32_t)s * cells + c] = __ldg(in.val + (uint32_t)s * cells + c);
@@ -464,40 +452,38 @@ __device__ __forceinline__ void process_cell(const In &in, const Out &out, const
         sl_ += (a - (s2 - bb)) + (b - bb);
         sh = s2;
     }
-    int cnt_out = 0;
+    // stored list: the phases that stay positive, ascending
+    int cnt_out = 0, id_first = LIQ;
     bool sovf = false;
-    if (sh + sl_ > 1e-20f) {
-        float inv = 1.0f / sh;
-        inv = inv - inv * inv * sl_;
-        for (int t = 0; t < n; ++t) {
-            const float v = outv[t] * inv;
-            if (v > 0.0f) {
-                if (cnt_out < S) {
-                    out.idx[(uint32_t)cnt_out * cells + c] = (uint16_t)A.ids[t];
-                    out.val[(uint32_t)cnt_out * cells + c] = v;
-                    ++cnt_out;
-                } else {
-                    sovf = true;
-                }
-            }
-        }
-    } else {
+    const bool normal = sh + sl_ > 1e-20f;
+    float inv = 1.0f / sh;
+    inv = inv - inv * inv * sl_;
+    if (!normal) {
         // all clipped to ~0: the liquid takes the cell (:679-680)
-        out.idx[c] = LIQ;
         out.val[c] = 1.0f;
+        id_first = LIQ;
         cnt_out = 1;
-        for (int t = 0; t < n; ++t) {
-            if (A.ids[t] == LIQ || !(outv[t] > 0.0f)) continue;
-            if (cnt_out < S) {
-                out.idx[(uint32_t)cnt_out * cells + c] = (uint16_t)A.ids[t];
-                out.val[(uint32_t)cnt_out * cells + c] = outv[t];
-                ++cnt_out;
-            } else {
-                sovf = true;
-            }
-        }
     }
-    out.cnt[c] = (uint8_t)cnt_out;
+    for (int t = 0; t < n; ++t) {
+        float v;
+        if (normal) {
+            v = outv[t] * inv;
+        } else {
+            if (A.ids[t] == LIQ) continue;
+            v = outv[t];
+        }
+        if (!(v > 0.0f)) continue;
+        if (cnt_out == S) {
+            sovf = true;
+            continue;
+        }
+        if (cnt_out == 0) id_first = A.ids[t];
+        else out.idx[(uint32_t)cnt_out * cells + c] = (uint16_t)A.ids[t];
+        out.val[(uint32_t)cnt_out * cells + c] = v;
+        ++cnt_out;
+    }
+    // one stored phase: its renormalised value is 1 and is left implicit
+    out.head[c] = mkhead(id_first, cnt_out, false);
     if (sovf) atomicOr(err, MPF3D_DEV_SLOT_OVERFLOW);
 }
 
@@ -523,43 +509,61 @@ __device__ __forceinline__ void push(const Queue &Q, int parity, bool want, bool
     }
 }
 
+constexpr int SWEEP_ZB = 4;  // cells per thread along z
+
 template <int S, int AMAX>
 __global__ void __launch_bounds__(256) sweep_kernel(In in, Out out, Mats M, Params P, Queue Q, int parity,
                                                     int32_t *__restrict__ err) {
     const int l = blockIdx.x * blockDim.x + threadIdx.x;
     const int m = blockIdx.y * blockDim.y + threadIdx.y;
-    const int k = blockIdx.z * blockDim.z + threadIdx.z;
+    const int k0 = (blockIdx.z * blockDim.z + threadIdx.z) * SWEEP_ZB;
     if (blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.x < 2 && threadIdx.y == 0 &&
         threadIdx.z == 0)
         Q.count[2 * (parity ^ 1) + threadIdx.x] = 0;  // the previous step's kernels are done with them
-    if (l >= P.nx || m >= P.ny || k >= P.nz) return;
-    const int lp = wrap_p(l, P.nx), lm = wrap_m(l, P.nx), mp = wrap_p(m, P.ny), mm = wrap_m(m, P.ny);
-    const int kp = clamp_p(k, P.nz), km = clamp_m(k, P.nz);
-    const uint32_t c = cidx(P, l, m, k);
-    const uint32_t nb[6] = {cidx(P, lp, m, k), cidx(P, lm, m, k), cidx(P, l, mp, k),
-                            cidx(P, l, mm, k), cidx(P, l, m, kp), cidx(P, l, m, km)};
-    const int c0 = __ldg(in.cnt + c);
-    const int i0 = __ldg(in.idx + c);
-    bool uniform = (c0 == 1);
-    bool liq = c0 > 0 && i0 == LIQ;
-    bool sol = c0 > 1 || (c0 == 1 && i0 != LIQ);
+    if (l >= P.nx || m >= P.ny || k0 >= P.nz) return;
+    const uint32_t plane = (uint32_t)P.nx * (uint32_t)P.ny;
+    const uint32_t col = (uint32_t)m * (uint32_t)P.nx + (uint32_t)l;
+    const uint32_t dxp = (l < P.nx - 1) ? 1u : (uint32_t)(1 - P.nx);
+    const uint32_t dxm = (l > 0) ? (uint32_t)-1 : (uint32_t)(P.nx - 1);
+    const uint32_t dyp = (m < P.ny - 1) ? (uint32_t)P.nx : (uint32_t)(-(P.ny - 1) * P.nx);
+    const uint32_t dym = (m > 0) ? (uint32_t)(-P.nx) : (uint32_t)((P.ny - 1) * P.nx);
+    // heads of the column k0-1 .. k0+ZB (z clamped)
+    uint32_t hz[SWEEP_ZB + 2];
 #pragma unroll
-    for (int p = 0; p < 6; ++p) {
-        const int cq = __ldg(in.cnt + nb[p]);
-        const int iq = __ldg(in.idx + nb[p]);
-        uniform = uniform && cq == 1 && iq == i0;
-        liq = liq || (cq > 0 && iq == LIQ);
-        sol = sol || cq > 1 || (cq == 1 && iq != LIQ);
+    for (int j = 0; j < SWEEP_ZB + 2; ++j) {
+        const int kk = min(max(k0 - 1 + j, 0), P.nz - 1);
+        hz[j] = __ldg(in.head + (uint32_t)kk * plane + col);
     }
-    if (uniform) {
-        out.cnt[c] = 1;
-        out.idx[c] = (uint16_t)i0;
-        out.val[c] = 1.0f;
-        return;
+#pragma unroll
+    for (int j = 0; j < SWEEP_ZB; ++j) {
+        const int k = k0 + j;
+        if (k >= P.nz) break;
+        const uint32_t c = (uint32_t)k * plane + col;
+        const uint32_t h0 = hz[j + 1];
+        uint32_t hn[6] = {__ldg(in.head + c + dxp), __ldg(in.head + c + dxm), __ldg(in.head + c + dyp),
+                                __ldg(in.head + c + dym), hz[j + 2], hz[j]};
+        // a z neighbour beyond the domain is the cell itself (clamped index)
+        if (k == P.nz - 1) hn[4] = h0;
+        if (k == 0) hn[5] = h0;
+        bool uniform = hcount(h0) == 1 && !hexplicit(h0);
+        bool liq = hcount(h0) > 0 && hid0(h0) == LIQ;
+        bool sol = hcount(h0) > 1 || (hcount(h0) == 1 && hid0(h0) != LIQ);
+#pragma unroll
+        for (int p = 0; p < 6; ++p) {
+            const uint32_t h = hn[p];
+            uniform = uniform && h == h0;
+            liq = liq || (hcount(h) > 0 && hid0(h) == LIQ);
+            sol = sol || hcount(h) > 1 || (hcount(h) == 1 && hid0(h) != LIQ);
+        }
+        if (uniform) {
+            // the one phase of the neighbourhood keeps the cell at exactly 1
+            out.head[c] = h0;
+        } else {
+            const bool heavy = liq && sol && P.use_aniso;
+            push(Q, parity, heavy, true, P.cells32, c);
+            push(Q, parity, !heavy, false, P.cells32, c);
+        }
     }
-    const bool heavy = liq && sol && P.use_aniso;
-    push(Q, parity, heavy, true, P.cells32, c);
-    push(Q, parity, !heavy, false, P.cells32, c);
 }
 
 // Kernel 2 of a step: the cells queued for the general update, one thread
@@ -609,14 +613,16 @@ __global__ void from_dense_kernel(const T *__restrict__ phi, int N, int nx, int 
     const int64_t src = ((int64_t)l * ny + m) * nz + k;
     const int64_t cells = plane;
     const int64_t dst = ((int64_t)k * ny + m) * nx + l;
-    int c = 0;
+    int c = 0, id0 = 0;
+    float v0 = 0.0f;
     bool bad = false, ovf = false;
     for (int g = 0; g < N; ++g) {
         const T v = phi[(int64_t)g * plane + src];
         if (!(v >= (T)0)) { bad = true; continue; }
         if (v > (T)0) {
             if (c < S) {
-                out.idx[c * cells + dst] = (uint16_t)g;
+                if (c == 0) { id0 = g; v0 = (float)v; }
+                else out.idx[c * cells + dst] = (uint16_t)g;
                 out.val[c * cells + dst] = (float)v;
             } else {
                 ovf = true;
@@ -624,7 +630,8 @@ __global__ void from_dense_kernel(const T *__restrict__ phi, int N, int nx, int 
             ++c;
         }
     }
-    out.cnt[dst] = (uint8_t)(c < S ? c : S);
+    const int n = c < S ? c : S;
+    out.head[dst] = mkhead(id0, n, n == 1 && v0 != 1.0f);
     if (bad) atomicOr(err, MPF3D_DEV_BAD_INPUT);
     if (ovf) atomicOr(err, MPF3D_DEV_SLOT_OVERFLOW);
 }
@@ -639,11 +646,12 @@ __global__ void to_dense_kernel(In in, int N, int nx, int ny, int nz, T *__restr
     const int64_t dstc = ((int64_t)l * ny + m) * nz + k;
     const int64_t srcc = ((int64_t)k * ny + m) * nx + l;
     for (int g = 0; g < N; ++g) phi[(int64_t)g * plane + dstc] = (T)0;
-    int c = in.cnt[srcc];
-    c = c < S ? c : S;
+    const uint32_t h = in.head[srcc];
+    const int c = min(hcount(h), S);
     for (int s = 0; s < c; ++s) {
-        const int g = in.idx[s * plane + srcc];
-        if (g < N) phi[(int64_t)g * plane + dstc] = (T)in.val[s * plane + srcc];
+        const int g = s == 0 ? hid0(h) : (int)in.idx[s * plane + srcc];
+        const float v = s == 0 ? value0(in, h, (uint32_t)srcc) : in.val[s * plane + srcc];
+        if (g < N) phi[(int64_t)g * plane + dstc] = (T)v;
     }
 }
 
@@ -657,9 +665,12 @@ __global__ void active_count_kernel(In in, int nx, int ny, int nz, int32_t *__re
     const int64_t cells = (int64_t)nx * ny * nz;
     const int lp = wrap_p(l, nx), lm = wrap_m(l, nx), mp = wrap_p(m, ny), mm = wrap_m(m, ny);
     const int kp = clamp_p(k, nz), km = clamp_m(k, nz);
-    auto cidx = [&](int a, int b, int d) { return ((int64_t)d * ny + b) * nx + a; };
-    const int64_t pt[7] = {cidx(l, m, k), cidx(lp, m, k), cidx(lm, m, k), cidx(l, mp, k),
-                           cidx(l, mm, k), cidx(l, m, kp), cidx(l, m, km)};
+    auto ci = [&](int a, int b, int d) { return ((int64_t)d * ny + b) * nx + a; };
+    const int64_t pt[7] = {ci(l, m, k), ci(lp, m, k), ci(lm, m, k), ci(l, mp, k),
+                           ci(l, mm, k), ci(l, m, kp), ci(l, m, km)};
+    auto id_at = [&](int p, int s) {
+        return s == 0 ? hid0(in.head[pt[p]]) : (int)in.idx[s * cells + pt[p]];
+    };
     // count distinct ids of the 7 sorted lists by repeated minimum extraction
     int pos[7];
     for (int p = 0; p < 7; ++p) pos[p] = 0;
@@ -667,10 +678,9 @@ __global__ void active_count_kernel(In in, int nx, int ny, int nz, int32_t *__re
     while (true) {
         int best = 1 << 30;
         for (int p = 0; p < 7; ++p) {
-            int c = in.cnt[pt[p]];
-            c = c < S ? c : S;
-            while (pos[p] < c && (int)in.idx[pos[p] * cells + pt[p]] <= last) ++pos[p];
-            if (pos[p] < c) best = min(best, (int)in.idx[pos[p] * cells + pt[p]]);
+            const int c = min(hcount(in.head[pt[p]]), S);
+            while (pos[p] < c && id_at(p, pos[p]) <= last) ++pos[p];
+            if (pos[p] < c) best = min(best, id_at(p, pos[p]));
         }
         if (best == (1 << 30)) break;
         last = best;
@@ -699,8 +709,8 @@ bool dims_ok(int nx, int ny, int nz) {
 template <int S, int AMAX>
 void launch_step(const In &in, const Out &out, const Mats &M, const Params &P, const Queue &Q, int parity,
                  int32_t *err, cudaStream_t s) {
-    dim3 blk(32, 4, 2);
-    dim3 grd((P.nx + 31) / 32, (P.ny + 3) / 4, (P.nz + 1) / 2);
+    dim3 blk(32, 8, 1);
+    dim3 grd((P.nx + 31) / 32, (P.ny + 7) / 8, (P.nz + SWEEP_ZB - 1) / SWEEP_ZB);
     sweep_kernel<S, AMAX><<<grd, blk, 0, s>>>(in, out, M, P, Q, parity, err);
     int dev = 0, sms = 148;
     cudaGetDevice(&dev);
@@ -712,7 +722,7 @@ void launch_step(const In &in, const Out &out, const Mats &M, const Params &P, c
 }  // namespace
 
 extern "C" int mpf3d_compact_from_dense(const void *phi, int phi_dtype, int N, int nx, int ny, int nz, int slots,
-                                        uint8_t *cnt, uint16_t *idx, float *val, int32_t *err, void *stream) {
+                                        uint32_t *cnt, uint16_t *idx, float *val, int32_t *err, void *stream) {
     if (!phi || !cnt || !idx || !val || !err || N <= 0 || N > 65535 || !dims_ok(nx, ny, nz)) return MPF3D_ERR_ARG;
     cudaStream_t s = (cudaStream_t)stream;
     dim3 b(32, 4, 2);
@@ -732,7 +742,7 @@ extern "C" int mpf3d_compact_from_dense(const void *phi, int phi_dtype, int N, i
     return cudaGetLastError() == cudaSuccess ? MPF3D_OK : MPF3D_ERR_CUDA;
 }
 
-extern "C" int mpf3d_compact_to_dense(const uint8_t *cnt, const uint16_t *idx, const float *val, int slots, int N,
+extern "C" int mpf3d_compact_to_dense(const uint32_t *cnt, const uint16_t *idx, const float *val, int slots, int N,
                                       int nx, int ny, int nz, void *phi, int phi_dtype, void *stream) {
     if (!phi || !cnt || !idx || !val || N <= 0 || N > 65535 || !dims_ok(nx, ny, nz)) return MPF3D_ERR_ARG;
     cudaStream_t s = (cudaStream_t)stream;
@@ -753,7 +763,7 @@ extern "C" int mpf3d_compact_to_dense(const uint8_t *cnt, const uint16_t *idx, c
     return cudaGetLastError() == cudaSuccess ? MPF3D_OK : MPF3D_ERR_CUDA;
 }
 
-extern "C" int mpf3d_compact_active_count(const uint8_t *cnt, const uint16_t *idx, int slots, int nx, int ny, int nz,
+extern "C" int mpf3d_compact_active_count(const uint32_t *cnt, const uint16_t *idx, int slots, int nx, int ny, int nz,
                                           int32_t *nf, void *stream) {
     if (!cnt || !idx || !nf || !dims_ok(nx, ny, nz)) return MPF3D_ERR_ARG;
     cudaStream_t s = (cudaStream_t)stream;
@@ -767,7 +777,7 @@ extern "C" int mpf3d_compact_active_count(const uint8_t *cnt, const uint16_t *id
     return cudaGetLastError() == cudaSuccess ? MPF3D_OK : MPF3D_ERR_CUDA;
 }
 
-extern "C" int mpf3d_compact_step(const uint8_t *cnt, const uint16_t *idx, const float *val, uint8_t *cnt_out,
+extern "C" int mpf3d_compact_step(const uint32_t *cnt, const uint16_t *idx, const float *val, uint32_t *cnt_out,
                                   uint16_t *idx_out, float *val_out, int slots, int amax, const double *T0z,
                                   double Tm_plus_cool, const float *wij, const float *a2ij, const float *mij,
                                   const float *n111, int N, int nx, int ny, int nz, const mpf3d_scalars *sc,

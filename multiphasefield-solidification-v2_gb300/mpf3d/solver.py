@@ -109,7 +109,7 @@ class CompactSolver:
     # -- buffers ---------------------------------------------------------------
     def _alloc(self):
         torch = _torch()
-        return (torch.empty(self.cells, dtype=torch.uint8, device=self.device),
+        return (torch.empty(self.cells, dtype=torch.int32, device=self.device),
                 torch.empty(self.slots * self.cells, dtype=torch.int16, device=self.device),
                 torch.empty(self.slots * self.cells, dtype=torch.float32, device=self.device))
 
@@ -215,7 +215,18 @@ class CompactSolver:
         return nf.cpu().numpy() if host else nf
 
     def stored_counts(self):
-        return self.buf[self.cur][0]
+        """Number of stored phases per cell (x-fastest order)."""
+        return self.buf[self.cur][0] & 0x7F
+
+    def record_bytes(self) -> int:
+        """Bytes of the current state that a step must read: the 4-byte head
+        of every cell plus 6 bytes per stored phase of cells holding two or
+        more (4 for an explicitly stored single value)."""
+        h = self.buf[self.cur][0]
+        n = (h & 0x7F).long()
+        e = ((h >> 7) & 1).long()
+        extra = _torch().where(n >= 2, 6 * n - 2, 4 * e)
+        return int(4 * self.cells + extra.sum().item())
 
     def state_bytes(self) -> int:
-        return self.cells * (1 + 6 * self.slots)
+        return self.cells * (4 + 6 * self.slots)
