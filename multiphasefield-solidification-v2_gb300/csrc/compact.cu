@@ -540,8 +540,11 @@ __global__ void __launch_bounds__(256) sweep_kernel(In in, Out out, Mats M, Para
         if (k >= P.nz) break;
         const uint32_t c = (uint32_t)k * plane + col;
         const uint32_t h0 = hz[j + 1];
-        uint32_t hn[6] = {__ldg(in.head + c + dxp), __ldg(in.head + c + dxm), __ldg(in.head + c + dyp),
-                                __ldg(in.head + c + dym), hz[j + 2], hz[j]};
+        // neighbour indices wrap in 32-bit cell-index arithmetic; the offsets
+        // must be added to the index, never to the pointer
+        const uint32_t qxp = c + dxp, qxm = c + dxm, qyp = c + dyp, qym = c + dym;
+        uint32_t hn[6] = {__ldg(in.head + qxp), __ldg(in.head + qxm), __ldg(in.head + qyp),
+                          __ldg(in.head + qym), hz[j + 2], hz[j]};
         // a z neighbour beyond the domain is the cell itself (clamped index)
         if (k == P.nz - 1) hn[4] = h0;
         if (k == 0) hn[5] = h0;
