@@ -252,7 +252,7 @@ __device__ __forceinline__ void gather(const In &in, const Params &P, const uint
 // a cell from the liquid gradient at the 7 points and the liquid's second
 // derivatives at the cell (aniso_term1_solid_3d :149-204, torque_A11_3d
 // :386-441, A13_divergence_3d :344-383, calc_b_from_cos :33-55).
-__device__ __noinline__ void interface_terms(const Params &P, const float3 (&G)[7], const float (&vL)[7],
+__device__ __forceinline__ void interface_terms(const Params &P, const float3 (&G)[7], const float (&vL)[7],
                                                 const float (&h2)[6], const float *__restrict__ u, bool torque,
                                                 float &lap_sl, float &b_sl) {
     Facet F[7];
