@@ -248,6 +248,45 @@ __device__ __forceinline__ void gather(const In &in, const Params &P, const uint
     }
 }
 
+// Facet-derived quantities of one grain at one stencil point: the
+// anisotropy a(theta) (calc_a_from_cos :24-30), eps^2 = (eps0 a)^2 and
+// d a / d(grad phi) (da_dphixyz_A12 :304-341).  C = sqrt(c^2+p^2) and
+// S = sqrt(max(1-c^2,0)+p^2) are shared by a and da/dc.
+struct PointTerms {
+    float e2;        // eps^2 at the point
+    float a;         // a(theta)
+    float3 da;       // d a / d(phi_x, phi_y, phi_z); zero below the floor
+    float coef;      // mu_a delta_a (c/C - tan(a0) c/S)
+};
+
+__device__ __forceinline__ PointTerms point_terms(const Params &P, float3 g, const Facet &f, bool want_da) {
+    PointTerms t;
+    if (!f.valid) {
+        t.e2 = P.e2_flat;
+        t.a = 0.0f;
+        t.da = make_float3(0.f, 0.f, 0.f);
+        t.coef = 0.0f;
+        return t;
+    }
+    const float c = f.cs, c2 = c * c;
+    const float C = sqrtf(c2 + P.pp);
+    const float S = sqrtf(fmaxf(1.0f - c2, 0.0f) + P.pp);
+    t.a = P.mu_a * (1.0f + P.delta_a * (C + P.tan_a0 * S));
+    const float e = P.eps0 * t.a;
+    t.e2 = e * e;
+    t.coef = P.mu_da * (__fdividef(c, C) - P.tan_a0 * __fdividef(c, S));
+    if (want_da) {
+        const float ig = rsqrtf(f.q);
+        const float ig3 = ig * ig * ig;
+        const float ud = g.x * f.nx + g.y * f.ny + g.z * f.nz;
+        t.da = make_float3(t.coef * (f.nx * ig - ud * g.x * ig3), t.coef * (f.ny * ig - ud * g.y * ig3),
+                           t.coef * (f.nz * ig - ud * g.z * ig3));
+    } else {
+        t.da = make_float3(0.f, 0.f, 0.f);
+    }
+    return t;
+}
+
 // eps^2-weighted divergence, torque and kinetic factor of one solid grain at
 // a cell from the liquid gradient at the 7 points and the liquid's second
 // derivatives at the cell (aniso_term1_solid_3d :149-204, torque_A11_3d
@@ -273,23 +312,21 @@ __device__ __forceinline__ void interface_terms(const Params &P, const float3 (&
         b_sl = P.b_flat;
         return;
     }
-    float e2[7];
+    const bool tq = torque && F[0].valid;
+    PointTerms T[7];
+    T[0] = point_terms(P, G[0], F[0], tq);
 #pragma unroll
-    for (int p = 0; p < 7; ++p) {
-        const float e = P.eps0 * calc_a(P, F[p].cabs);
-        e2[p] = F[p].valid ? e * e : P.e2_flat;
-    }
-    float lv = ((e2[0] + e2[1]) * (vL[1] - Lc) - (e2[0] + e2[2]) * (Lc - vL[2])) * h +
-               ((e2[0] + e2[3]) * (vL[3] - Lc) - (e2[0] + e2[4]) * (Lc - vL[4])) * h +
-               ((e2[0] + e2[5]) * (vL[5] - Lc) - (e2[0] + e2[6]) * (Lc - vL[6])) * h;
-    if (torque && F[0].valid) {
+    for (int p = 1; p < 7; ++p) T[p] = point_terms(P, G[p], F[p], tq);
+    float lv = ((T[0].e2 + T[1].e2) * (vL[1] - Lc) - (T[0].e2 + T[2].e2) * (Lc - vL[2])) * h +
+               ((T[0].e2 + T[3].e2) * (vL[3] - Lc) - (T[0].e2 + T[4].e2) * (Lc - vL[4])) * h +
+               ((T[0].e2 + T[5].e2) * (vL[5] - Lc) - (T[0].e2 + T[6].e2) * (Lc - vL[6])) * h;
+    if (tq) {
         const float3 g0 = G[0];
         const float q = F[0].q;
         const float pxx = h2[0], pyy = h2[1], pzz = h2[2], pxy = h2[3], pxz = h2[4], pyz = h2[5];
         const float qx = 2.0f * (g0.x * pxx + g0.y * pxy + g0.z * pxz);
         const float qy = 2.0f * (g0.x * pxy + g0.y * pyy + g0.z * pyz);
         const float qz = 2.0f * (g0.x * pxz + g0.y * pyz + g0.z * pzz);
-        const float4 d0 = da_dgrad(P, g0, F[0]);
         const float ig = rsqrtf(q), ig3 = ig * ig * ig;
         const float ud = g0.x * F[0].nx + g0.y * F[0].ny + g0.z * F[0].nz;
         const float dcx = F[0].nx * ig - ud * g0.x * ig3;
@@ -298,15 +335,16 @@ __device__ __forceinline__ void interface_terms(const Params &P, const float3 (&
         const float cxx = dcx * pxx + dcy * pxy + dcz * pxz;
         const float cyy = dcx * pxy + dcy * pyy + dcz * pyz;
         const float czz = dcx * pxz + dcy * pyz + dcz * pzz;
-        const float cs = F[0].cs, cs2 = cs * cs;
-        const float coef = P.mu_da * (cs / sqrtf(cs2 + P.pp) - P.tan_a0 * (cs / sqrtf(fmaxf(1.0f - cs2, 0.0f) + P.pp)));
-        const float ddx = (da_dgrad(P, G[1], F[1]).y - da_dgrad(P, G[2], F[2]).y) * P.half_over_dx;
-        const float ddy = (da_dgrad(P, G[3], F[3]).z - da_dgrad(P, G[4], F[4]).z) * P.half_over_dx;
-        const float ddz = (da_dgrad(P, G[5], F[5]).w - da_dgrad(P, G[6], F[6]).w) * P.half_over_dx;
-        const float a = d0.x;
-        const float Ex = coef * cxx * d0.y * q + a * ddx * q + a * d0.y * qx;
-        const float Ey = coef * cyy * d0.z * q + a * ddy * q + a * d0.z * qy;
-        const float Ez = coef * czz * d0.w * q + a * ddz * q + a * d0.w * qz;
+        const float coef = T[0].coef;
+        // A13_divergence_3d: central differences of da/dphi_p at the neighbours
+        const float ddx = (T[1].da.x - T[2].da.x) * P.half_over_dx;
+        const float ddy = (T[3].da.y - T[4].da.y) * P.half_over_dx;
+        const float ddz = (T[5].da.z - T[6].da.z) * P.half_over_dx;
+        const float a = T[0].a;
+        const float3 d0 = T[0].da;
+        const float Ex = coef * cxx * d0.x * q + a * ddx * q + a * d0.x * qx;
+        const float Ey = coef * cyy * d0.y * q + a * ddy * q + a * d0.y * qy;
+        const float Ez = coef * czz * d0.z * q + a * ddz * q + a * d0.z * qz;
         lv += P.eps0sq * (Ex + Ey + Ez);
     }
     lap_sl = lv;
