@@ -132,6 +132,30 @@ int mpf3d_compact_step(const uint32_t *head, const uint16_t *idx, const float *v
                        uint32_t *work_items, uint32_t *work_count, int parity, int32_t *err,
                        void *stream);
 
+/* Largest grid (nx*ny*nz) that mpf3d_compact_step_noalloc accepts. */
+#define MPF3D_NOALLOC_MAX_CELLS 4194304u
+
+/* mpf3d_compact_step without caller scratch and without any device
+ * allocation.  No counterpart in the reference: it serves hosts that cannot
+ * let a library allocate device memory -- applications that reserve the whole
+ * memory budget up front for their own pool, or real-time loops where a
+ * cudaMalloc (which may synchronise the device) is not acceptable.
+ * The step's work list lives in a file-scope device array of
+ * MPF3D_NOALLOC_MAX_CELLS entries (16 MiB, plus 16 bytes of counters) that
+ * every GPU loading the library holds until the process exits; larger grids
+ * return MPF3D_ERR_TOO_LARGE.  The first call on a device looks up the
+ * array's device address with that device current; make that first call
+ * before any stream capture.  All calls share the array and the call clears
+ * its counters on `stream` first, so calls that overlap on the GPU (other
+ * streams, other host threads) race on it: serialise them.  Other arguments
+ * and results are those of mpf3d_compact_step (parity is not needed). */
+int mpf3d_compact_step_noalloc(const uint32_t *head, const uint16_t *idx, const float *val,
+                               uint32_t *head_out, uint16_t *idx_out, float *val_out, int slots, int amax,
+                               const double *T0z, double Tm_plus_cool, const float *wij, const float *a2ij,
+                               const float *mij, const float *n111, int N, int nx, int ny, int nz,
+                               const mpf3d_scalars *scalars, int enable_anisotropy, int enable_torque,
+                               int symmetric_normals, int32_t *err, void *stream);
+
 /* library version, for the binding's load check */
 int mpf3d_version(void);
 

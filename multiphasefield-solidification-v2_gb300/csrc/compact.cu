@@ -24,6 +24,8 @@
 #include <math.h>
 #include <stdint.h>
 
+#include <mutex>
+
 #include "mpf3d.h"
 #include "mpf3d_internal.h"
 
@@ -885,4 +887,71 @@ extern "C" int mpf3d_compact_step(const uint32_t *cnt, const uint16_t *idx, cons
     else if (slots == 16 && amax == 32) launch_step<16, 32>(in, out, M, P, Q, parity, err, s);
     else return MPF3D_ERR_ARG;
     return cudaGetLastError() == cudaSuccess ? MPF3D_OK : MPF3D_ERR_CUDA;
+}
+
+// ---------------------------------------------------------------------------
+// Step without device allocation.
+//
+// Some hosts cannot let this library allocate device memory: applications
+// that reserve the whole GPU memory budget up front for their own pool and
+// give plugins none, or real-time loops where a cudaMalloc -- which may
+// synchronise the device -- is not acceptable.  For them the work list of
+// the step lives in a file-scope device array instead of caller scratch.
+// Every GPU that loads the library holds the array until the process exits.
+namespace {
+
+constexpr uint32_t kNoAllocMaxCells = MPF3D_NOALLOC_MAX_CELLS;
+constexpr int kNoAllocMaxDevices = 64;
+
+static __device__ __align__(256) uint32_t g_noalloc_items[kNoAllocMaxCells];
+static __device__ __align__(256) uint32_t g_noalloc_count[4];
+
+struct NoAllocScratch {
+    uint32_t *items = nullptr;
+    uint32_t *count = nullptr;
+    bool ready = false;
+};
+NoAllocScratch g_noalloc_dev[kNoAllocMaxDevices];
+std::mutex g_noalloc_mu;
+
+// Device addresses of the array on the current device.  In host code the
+// array's name is only a host-side stand-in, so the address is looked up
+// once per device, with that device current.
+int noalloc_scratch(uint32_t **items, uint32_t **count) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return MPF3D_ERR_CUDA;
+    if (dev < 0 || dev >= kNoAllocMaxDevices) return MPF3D_ERR_ARG;
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    NoAllocScratch &s = g_noalloc_dev[dev];
+    if (!s.ready) {
+        void *pi = nullptr, *pc = nullptr;
+        if (cudaGetSymbolAddress(&pi, g_noalloc_items) != cudaSuccess) return MPF3D_ERR_CUDA;
+        if (cudaGetSymbolAddress(&pc, g_noalloc_count) != cudaSuccess) return MPF3D_ERR_CUDA;
+        s.items = (uint32_t *)pi;
+        s.count = (uint32_t *)pc;
+        s.ready = true;
+    }
+    *items = s.items;
+    *count = s.count;
+    return MPF3D_OK;
+}
+
+}  // namespace
+
+extern "C" int mpf3d_compact_step_noalloc(const uint32_t *head, const uint16_t *idx, const float *val,
+                                          uint32_t *head_out, uint16_t *idx_out, float *val_out, int slots,
+                                          int amax, const double *T0z, double Tm_plus_cool, const float *wij,
+                                          const float *a2ij, const float *mij, const float *n111, int N, int nx,
+                                          int ny, int nz, const mpf3d_scalars *sc, int enable_anisotropy,
+                                          int enable_torque, int symmetric_normals, int32_t *err, void *stream) {
+    if (nx <= 0 || ny <= 0 || nz <= 0) return MPF3D_ERR_ARG;
+    if ((int64_t)nx * ny * nz > (int64_t)kNoAllocMaxCells) return MPF3D_ERR_TOO_LARGE;
+    uint32_t *items = nullptr, *count = nullptr;
+    const int rc = noalloc_scratch(&items, &count);
+    if (rc != MPF3D_OK) return rc;
+    // the counters must start at zero; the previous call left its totals there
+    if (cudaMemsetAsync(count, 0, 4 * sizeof(uint32_t), (cudaStream_t)stream) != cudaSuccess) return MPF3D_ERR_CUDA;
+    return mpf3d_compact_step(head, idx, val, head_out, idx_out, val_out, slots, amax, T0z, Tm_plus_cool, wij,
+                              a2ij, mij, n111, N, nx, ny, nz, sc, enable_anisotropy, enable_torque,
+                              symmetric_normals, items, count, 0, err, stream);
 }

@@ -45,6 +45,9 @@ _SIGS = {
     "mpf3d_compact_step": (_I32, [_VP, _VP, _VP, _VP, _VP, _VP, _I32, _I32, _VP, _F64, _VP, _VP, _VP, _VP,
                                   _I32, _I32, _I32, _I32, ctypes.POINTER(Scalars), _I32, _I32, _I32,
                                   _VP, _VP, _I32, _VP, _VP]),
+    "mpf3d_compact_step_noalloc": (_I32, [_VP, _VP, _VP, _VP, _VP, _VP, _I32, _I32, _VP, _F64, _VP, _VP,
+                                          _VP, _VP, _I32, _I32, _I32, _I32, ctypes.POINTER(Scalars),
+                                          _I32, _I32, _I32, _VP, _VP]),
 }
 
 _LIB = None
