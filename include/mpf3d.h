@@ -132,6 +132,70 @@ int mpf3d_compact_step(const uint32_t *head, const uint16_t *idx, const float *v
                        uint32_t *work_items, uint32_t *work_count, int parity, int32_t *err,
                        void *stream);
 
+/* compact state -> dense phi of one domain stored at cells [base, base +
+ * nx*ny*nz) of state arrays whose slot planes are `stride` cells apart. */
+int mpf3d_compact_to_dense_view(const uint32_t *head, const uint16_t *idx, const float *val, int slots,
+                                uint32_t stride, uint32_t base, int N, int nx, int ny, int nz, void *phi,
+                                int phi_dtype, void *stream);
+
+/* ---- batched instances (bicrystal / orientation-scan batches) -----------
+ * No reference counterpart: the reference runs one domain at a time
+ * (run_orientation_scan_3d.py:686-841, tests/verification_3d.py:1951-2011).
+ * Instances share one compact state; instance i owns cells [offset,
+ * offset + nx*ny*nz).  The table lives in DEVICE memory, sorted by offset
+ * and tile_start, where tile_start is the first sweep tile of the instance
+ * (tiles are 32 x 8 x 4 cells: ceil(nx/32)*ceil(ny/8)*ceil(nz/4) per
+ * instance).  Temperature is uniform per instance (T_melt - undercooling),
+ * anisotropy strength and grain orientations per instance. */
+typedef struct mpf3d_instance {
+    int32_t nx, ny, nz;
+    uint32_t offset;      /* first cell of the instance */
+    int32_t n111_base;    /* first n111 row of the instance's phases */
+    int32_t split;        /* bicrystal: grain 1 for x < split, grain 2 for x >= split */
+    int32_t tile_start;   /* first sweep tile of the instance */
+    float delta_a;        /* anisotropy strength */
+    float mu_da;          /* float(mu_a * delta_a) */
+    float e2_flat;        /* float((eps0_sl * a(theta at cos 0))^2) for this delta_a */
+    float undercooling;   /* T_melt - T */
+    float base_height;    /* bicrystal: initial solid height in cells */
+} mpf3d_instance;
+
+/* Bicrystal initial state of every instance: a tanh solid base of
+ * base_height cells (src/seed_modes_3d.py:46-56 profile), grain 1 left of
+ * `split`, grain 2 right of it, liquid above. */
+int mpf3d_batched_init_bicrystal(const mpf3d_instance *inst, int n_inst, uint32_t total_cells, double dx,
+                                 double delta, uint32_t *head, uint16_t *idx, float *val, int32_t *err,
+                                 void *stream);
+
+/* One step of every instance: the three step kernels of mpf3d_compact_step
+ * launched once over the whole batch.  n_tiles = total sweep tiles.  Shared
+ * physics from `scalars` (delta_a there is ignored); the rest as
+ * mpf3d_compact_step with total_cells in place of nx*ny*nz. */
+int mpf3d_batched_step(const uint32_t *head, const uint16_t *idx, const float *val, uint32_t *head_out,
+                       uint16_t *idx_out, float *val_out, int slots, int amax, const mpf3d_instance *inst,
+                       int n_inst, int n_tiles, uint32_t total_cells, const float *wij, const float *a2ij,
+                       const float *mij, const float *n111, int N, const mpf3d_scalars *scalars,
+                       int enable_anisotropy, int enable_torque, int symmetric_normals, uint32_t *work_items,
+                       uint32_t *work_count, int parity, int32_t *err, void *stream);
+
+/* Observables per instance, accumulated into zeroed float64 arrays:
+ * acc[6*i..6*i+5] = {sum of front heights left of split, columns left, sum
+ * right, columns right, sum phi1, sum phi2}; the front of a column is the
+ * highest z whose solid fraction exceeds 0.5 (interface_positions_3d,
+ * tests/verification_3d.py:409-416). */
+int mpf3d_batched_fronts(const uint32_t *head, const uint16_t *idx, const float *val, int slots,
+                         const mpf3d_instance *inst, int n_inst, uint32_t total_cells, double *acc,
+                         void *stream);
+
+/* Grain-boundary rows: for every z row of every instance with solid
+ * fraction >= 0.15, the phi1 = phi2 crossing along x nearest `split`
+ * (measure_gb_inclination, tests/run_paper_verification.py:658-723) summed
+ * over y: gb[2*(row_base[i] + k)] += x, gb[2*(row_base[i] + k) + 1] += 1.
+ * row_base (device, int32[n_inst]) = running sum of nz. */
+int mpf3d_batched_gb_rows(const uint32_t *head, const uint16_t *idx, const float *val, int slots,
+                          const mpf3d_instance *inst, int n_inst, uint32_t total_cells, const int32_t *row_base,
+                          double *gb, void *stream);
+
 /* Largest grid (nx*ny*nz) that mpf3d_compact_step_noalloc accepts. */
 #define MPF3D_NOALLOC_MAX_CELLS 4194304u
 

@@ -24,6 +24,8 @@
 #include <math.h>
 #include <stdint.h>
 
+#include <string.h>
+
 #include <mutex>
 
 #include "mpf3d.h"
@@ -46,6 +48,11 @@ struct Params {
     double Tmc;  // T_melt + accumulated cooling (float64)
     int use_aniso, use_torque;
     int sym_normals;  // every grain's n111 rows 4..7 are -(rows 3..0)
+    // per-domain view (a batch of instances shares the state arrays)
+    uint32_t base;    // index of the domain's first cell in the state arrays
+    int n111_base;    // first n111 row of the domain's phases
+    int t_uniform;    // temperature uniform in the domain ...
+    float dT_uniform; // ... with T - T_melt = dT_uniform
 };
 
 struct In {
@@ -172,7 +179,7 @@ struct Mats {
 };
 
 __device__ __forceinline__ uint32_t cidx(const Params &P, int l, int m, int k) {
-    return ((uint32_t)k * (uint32_t)P.ny + (uint32_t)m) * (uint32_t)P.nx + (uint32_t)l;
+    return P.base + ((uint32_t)k * (uint32_t)P.ny + (uint32_t)m) * (uint32_t)P.nx + (uint32_t)l;
 }
 
 __device__ __forceinline__ float liquid32(const In &in, uint32_t q) {
@@ -424,9 +431,11 @@ __device__ __forceinline__ void process_cell(const In &in, const Out &out, const
             h2[4] = (Lxpzp - Lxpzm - Lxmzp + Lxmzm) * qq;
             h2[5] = (Lypzp - Lypzm - Lymzp + Lymzm) * qq;
             for (int t = 1; t < n; ++t)
-                interface_terms(P, G, A.vL, h2, M.n111 + (size_t)A.ids[t] * 24, P.use_torque != 0, lap_sl[t], b_sl[t]);
+                interface_terms(P, G, A.vL, h2, M.n111 + (size_t)(P.n111_base + A.ids[t]) * 24, P.use_torque != 0,
+                                lap_sl[t], b_sl[t]);
             if (A.ts > 0) {
-                const Facet fs = facet(A.gs, M.n111 + (size_t)A.ids[A.ts] * 24, P.g2_floor, P.sym_normals != 0);
+                const Facet fs = facet(A.gs, M.n111 + (size_t)(P.n111_base + A.ids[A.ts]) * 24, P.g2_floor,
+                                       P.sym_normals != 0);
                 const float al = calc_a(P, fs.cabs);
                 w_sl = P.w0 * (al * al);
             }
@@ -461,7 +470,7 @@ __device__ __forceinline__ void process_cell(const In &in, const Out &out, const
         W[t1] = w;
         Ag[t1] = a;
     }
-    const float dT = (float)(M.T0z[k] - P.Tmc);
+    const float dT = P.t_uniform ? P.dT_uniform : (float)(M.T0z[k] - P.Tmc);
     const float inv_n = 1.0f / (float)(n > 0 ? n : 1);
     float outv[AMAX];
     for (int t1 = 0; t1 < n; ++t1) {
@@ -551,18 +560,11 @@ __device__ __forceinline__ void push(const Queue &Q, int parity, bool want, bool
 
 constexpr int SWEEP_ZB = 4;  // cells per thread along z
 
-template <int S, int AMAX>
-__global__ void __launch_bounds__(256) sweep_kernel(In in, Out out, Mats M, Params P, Queue Q, int parity,
-                                                    int32_t *__restrict__ err) {
-    const int l = blockIdx.x * blockDim.x + threadIdx.x;
-    const int m = blockIdx.y * blockDim.y + threadIdx.y;
-    const int k0 = (blockIdx.z * blockDim.z + threadIdx.z) * SWEEP_ZB;
-    if (blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.x < 2 && threadIdx.y == 0 &&
-        threadIdx.z == 0)
-        Q.count[2 * (parity ^ 1) + threadIdx.x] = 0;  // the previous step's kernels are done with them
-    if (l >= P.nx || m >= P.ny || k0 >= P.nz) return;
+// The sweep of one column of SWEEP_ZB cells (l, m, k0..k0+ZB-1) of a domain.
+__device__ __forceinline__ void sweep_column(const In &in, const Out &out, const Params &P, const Queue &Q, int parity,
+                                             int l, int m, int k0) {
     const uint32_t plane = (uint32_t)P.nx * (uint32_t)P.ny;
-    const uint32_t col = (uint32_t)m * (uint32_t)P.nx + (uint32_t)l;
+    const uint32_t col = P.base + (uint32_t)m * (uint32_t)P.nx + (uint32_t)l;
     const uint32_t dxp = (l < P.nx - 1) ? 1u : (uint32_t)(1 - P.nx);
     const uint32_t dxm = (l > 0) ? (uint32_t)-1 : (uint32_t)(P.nx - 1);
     const uint32_t dyp = (m < P.ny - 1) ? (uint32_t)P.nx : (uint32_t)(-(P.ny - 1) * P.nx);
@@ -607,6 +609,19 @@ __global__ void __launch_bounds__(256) sweep_kernel(In in, Out out, Mats M, Para
             push(Q, parity, !heavy, false, P.cells32, c);
         }
     }
+}
+
+template <int S, int AMAX>
+__global__ void __launch_bounds__(256) sweep_kernel(In in, Out out, Mats M, Params P, Queue Q, int parity,
+                                                    int32_t *__restrict__ err) {
+    const int l = blockIdx.x * blockDim.x + threadIdx.x;
+    const int m = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k0 = (blockIdx.z * blockDim.z + threadIdx.z) * SWEEP_ZB;
+    if (blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.x < 2 && threadIdx.y == 0 &&
+        threadIdx.z == 0)
+        Q.count[2 * (parity ^ 1) + threadIdx.x] = 0;  // the previous step's kernels are done with them
+    if (l >= P.nx || m >= P.ny || k0 >= P.nz) return;
+    sweep_column(in, out, P, Q, parity, l, m, k0);
 }
 
 // Kernel 2 of a step: the cells queued for the general update, one thread
@@ -680,20 +695,21 @@ __global__ void from_dense_kernel(const T *__restrict__ phi, int N, int nx, int 
 }
 
 template <typename T, int S>
-__global__ void to_dense_kernel(In in, int N, int nx, int ny, int nz, T *__restrict__ phi) {
+__global__ void to_dense_kernel(In in, int N, int nx, int ny, int nz, uint32_t stride, uint32_t base,
+                                T *__restrict__ phi) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     const int m = blockIdx.y * blockDim.y + threadIdx.y;
     const int l = blockIdx.z * blockDim.z + threadIdx.z;
     if (k >= nz || m >= ny || l >= nx) return;
     const int64_t plane = (int64_t)nx * ny * nz;
     const int64_t dstc = ((int64_t)l * ny + m) * nz + k;
-    const int64_t srcc = ((int64_t)k * ny + m) * nx + l;
+    const uint32_t srcc = base + ((uint32_t)k * (uint32_t)ny + (uint32_t)m) * (uint32_t)nx + (uint32_t)l;
     for (int g = 0; g < N; ++g) phi[(int64_t)g * plane + dstc] = (T)0;
     const uint32_t h = in.head[srcc];
     const int c = min(hcount(h), S);
     for (int s = 0; s < c; ++s) {
-        const int g = s == 0 ? hid0(h) : (int)in.idx[s * plane + srcc];
-        const float v = s == 0 ? value0(in, h, (uint32_t)srcc) : in.val[s * plane + srcc];
+        const int g = s == 0 ? hid0(h) : (int)in.idx[(size_t)s * stride + srcc];
+        const float v = s == 0 ? value0(in, h, srcc) : in.val[(size_t)s * stride + srcc];
         if (g < N) phi[(int64_t)g * plane + dstc] = (T)v;
     }
 }
@@ -730,6 +746,195 @@ __global__ void active_count_kernel(In in, int nx, int ny, int nz, int32_t *__re
         ++n;
     }
     nf[((int64_t)l * ny + m) * nz + k] = n;
+}
+
+
+// ---------------------------------------------------------------------------
+// Batches of independent domains ("instances") sharing one set of state
+// arrays: instance i owns cells [offset, offset + nx*ny*nz) of every array.
+// One launch of each step kernel covers all instances; tiles and queued
+// cells find their instance by binary search over the instance table.
+
+__device__ __forceinline__ int find_instance_by_tile(const mpf3d_instance *__restrict__ inst, int n, int tile) {
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(&inst[mid].tile_start) <= tile) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ int find_instance_by_cell(const mpf3d_instance *__restrict__ inst, int n, uint32_t c) {
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(&inst[mid].offset) <= c) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ Params instance_params(const Params &P0, const mpf3d_instance &I) {
+    Params P = P0;
+    P.nx = I.nx; P.ny = I.ny; P.nz = I.nz;
+    P.base = I.offset;
+    P.n111_base = I.n111_base;
+    P.delta_a = I.delta_a;
+    P.mu_da = I.mu_da;
+    P.e2_flat = I.e2_flat;
+    P.t_uniform = 1;
+    P.dT_uniform = -I.undercooling;
+    return P;
+}
+
+template <int S, int AMAX>
+__global__ void __launch_bounds__(256) batched_sweep_kernel(In in, Out out, Params P0,
+                                                            const mpf3d_instance *__restrict__ inst, int n_inst,
+                                                            Queue Q, int parity) {
+    if (blockIdx.x == 0 && threadIdx.x < 2 && threadIdx.y == 0) Q.count[2 * (parity ^ 1) + threadIdx.x] = 0;
+    const int i = find_instance_by_tile(inst, n_inst, (int)blockIdx.x);
+    const mpf3d_instance I = inst[i];
+    const int t = (int)blockIdx.x - I.tile_start;
+    const int tx = (I.nx + 31) / 32, ty = (I.ny + 7) / 8;
+    const int l = (t % tx) * 32 + threadIdx.x;
+    const int m = ((t / tx) % ty) * 8 + threadIdx.y;
+    const int k0 = (t / (tx * ty)) * SWEEP_ZB;
+    if (l >= I.nx || m >= I.ny || k0 >= I.nz) return;
+    const Params P = instance_params(P0, I);
+    sweep_column(in, out, P, Q, parity, l, m, k0);
+}
+
+template <int S, int AMAX, bool HEAVY>
+__global__ void __launch_bounds__(HEAVY ? 128 : 256) batched_queue_kernel(In in, Out out, Mats M, Params P0,
+                                                                          const mpf3d_instance *__restrict__ inst,
+                                                                          int n_inst, Queue Q, int parity,
+                                                                          int32_t *__restrict__ err) {
+    const uint32_t n = *(volatile uint32_t *)(Q.count + 2 * parity + (HEAVY ? 1 : 0));
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t c = HEAVY ? Q.items[P0.cells32 - 1u - i] : Q.items[i];
+        const mpf3d_instance I = inst[find_instance_by_cell(inst, n_inst, c)];
+        const Params P = instance_params(P0, I);
+        const uint32_t r0 = c - I.offset;
+        const uint32_t plane = (uint32_t)I.nx * (uint32_t)I.ny;
+        const int k = (int)(r0 / plane);
+        const uint32_t r = r0 - (uint32_t)k * plane;
+        const int m = (int)(r / (uint32_t)I.nx);
+        const int l = (int)(r - (uint32_t)m * (uint32_t)I.nx);
+        process_cell<S, AMAX, HEAVY>(in, out, M, P, err, l, m, k);
+    }
+}
+
+// Initial bicrystal: a solid base of height base_height (tanh profile
+// 0.5*(1 - tanh(2.2/delta*(k - h)*dz)), as src/seed_modes_3d.py:46-56), grain
+// 1 for x < split and grain 2 for x >= split, liquid = clip(1 - solid).
+__global__ void batched_init_bicrystal_kernel(Out out, const mpf3d_instance *__restrict__ inst, int n_inst,
+                                              uint32_t stride, float factor_dz, int32_t *__restrict__ err) {
+    const int i = blockIdx.y;
+    if (i >= n_inst) return;
+    const mpf3d_instance I = inst[i];
+    const uint32_t cells = (uint32_t)I.nx * I.ny * I.nz;
+    for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < cells; r += gridDim.x * blockDim.x) {
+        const uint32_t plane = (uint32_t)I.nx * I.ny;
+        const int k = (int)(r / plane);
+        const int l = (int)((r - (uint32_t)k * plane) % (uint32_t)I.nx);
+        const float s = (float)(0.5 * (1.0 - tanh((double)factor_dz * ((double)k - (double)I.base_height))));
+        const float liq = fminf(fmaxf(1.0f - s, 0.0f), 1.0f);
+        const int g = l < I.split ? 1 : 2;
+        const uint32_t c = I.offset + r;
+        int n = 0, id0 = 0;
+        float v0 = 0.0f;
+        if (liq > 0.0f) { id0 = LIQ; v0 = liq; out.val[c] = liq; n = 1; }
+        if (s > 0.0f) {
+            if (n == 0) { id0 = g; v0 = s; out.val[c] = s; }
+            else { out.idx[(size_t)stride + c] = (uint16_t)g; out.val[(size_t)stride + c] = s; }
+            ++n;
+        }
+        out.head[c] = mkhead(id0, n, n == 1 && v0 != 1.0f);
+    }
+}
+
+// stored fraction of phase g at cell c (0 if not stored)
+template <int S>
+__device__ __forceinline__ float phase_at(const In &in, uint32_t stride, uint32_t c, int g) {
+    const uint32_t h = __ldg(in.head + c);
+    const int n = min(hcount(h), S);
+    if (n == 0) return 0.0f;
+    if (hid0(h) == g) return value0(in, h, c);
+    for (int s = 1; s < n; ++s)
+        if ((int)__ldg(in.idx + (size_t)s * stride + c) == g) return __ldg(in.val + (size_t)s * stride + c);
+    return 0.0f;
+}
+
+// Per instance: mean front height of each grain half (highest z with solid
+// fraction > 0.5 per column, interface_positions_3d of
+// tests/verification_3d.py:409-416) and the total fraction of grains 1, 2.
+// acc[6*i + ...] = {sum h left, columns left, sum h right, columns right, V1, V2}
+template <int S>
+__global__ void batched_fronts_kernel(In in, const mpf3d_instance *__restrict__ inst, int n_inst, uint32_t stride,
+                                      double *__restrict__ acc) {
+    const int i = blockIdx.y;
+    const mpf3d_instance I = inst[i];
+    const int cols = I.nx * I.ny;
+    const uint32_t plane = (uint32_t)cols;
+    double hl = 0.0, nl = 0.0, hr = 0.0, nr = 0.0, v1 = 0.0, v2 = 0.0;
+    for (int col = blockIdx.x * blockDim.x + threadIdx.x; col < cols; col += gridDim.x * blockDim.x) {
+        const int l = col % I.nx;
+        int front = -1;
+        for (int k = I.nz - 1; k >= 0; --k) {
+            const uint32_t c = I.offset + (uint32_t)k * plane + (uint32_t)col;
+            const float solid = 1.0f - phase_at<S>(in, stride, c, LIQ);
+            if (front < 0 && solid > 0.5f) front = k;
+            v1 += phase_at<S>(in, stride, c, 1);
+            v2 += phase_at<S>(in, stride, c, 2);
+        }
+        if (front >= 0) {
+            if (l < I.split) { hl += front; nl += 1.0; }
+            else { hr += front; nr += 1.0; }
+        }
+    }
+    double vals[6] = {hl, nl, hr, nr, v1, v2};
+#pragma unroll
+    for (int q = 0; q < 6; ++q) {
+        double v = vals[q];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if ((threadIdx.x & 31) == 0) atomicAdd(acc + 6 * i + q, v);
+    }
+}
+
+// Per instance and z row: the phi1 = phi2 crossing along x nearest the
+// initial split, averaged over y, for rows whose solid fraction is >= 0.15
+// (the grain-boundary locator of measure_gb_inclination,
+// tests/run_paper_verification.py:658-723, with a linear root between the
+// two cells of the sign change).  gb[2*(row_base + k) + {0,1}] = {sum x, rows}.
+template <int S>
+__global__ void batched_gb_rows_kernel(In in, const mpf3d_instance *__restrict__ inst, int n_inst, uint32_t stride,
+                                       const int *__restrict__ row_base, double *__restrict__ gb) {
+    const int i = blockIdx.y;
+    const mpf3d_instance I = inst[i];
+    const int rows = I.ny * I.nz;
+    const uint32_t plane = (uint32_t)I.nx * I.ny;
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += gridDim.x * blockDim.x) {
+        const int m = r % I.ny, k = r / I.ny;
+        const uint32_t row0 = I.offset + (uint32_t)k * plane + (uint32_t)m * I.nx;
+        float solid = 0.0f, best_x = 0.0f, best_d = 1e30f;
+        bool found = false;
+        float dprev = phase_at<S>(in, stride, row0, 1) - phase_at<S>(in, stride, row0, 2);
+        solid += 1.0f - phase_at<S>(in, stride, row0, LIQ);
+        for (int l = 1; l < I.nx; ++l) {
+            const uint32_t c = row0 + (uint32_t)l;
+            const float d = phase_at<S>(in, stride, c, 1) - phase_at<S>(in, stride, c, 2);
+            solid += 1.0f - phase_at<S>(in, stride, c, LIQ);
+            if ((dprev > 0.0f && d <= 0.0f) || (dprev < 0.0f && d >= 0.0f)) {
+                const float x = (float)(l - 1) + dprev / (dprev - d);
+                const float dist = fabsf(x - (float)I.split);
+                if (dist < best_d) { best_d = dist; best_x = x; found = true; }
+            }
+            dprev = d;
+        }
+        if (found && solid >= 0.15f * I.nx) {
+            atomicAdd(gb + 2 * (row_base[i] + k), (double)best_x);
+            atomicAdd(gb + 2 * (row_base[i] + k) + 1, 1.0);
+        }
+    }
 }
 
 }  // namespace compact
@@ -792,7 +997,7 @@ extern "C" int mpf3d_compact_to_dense(const uint32_t *cnt, const uint16_t *idx, 
     dim3 b(32, 4, 2);
     dim3 g = zfast_grid(nx, ny, nz, b);
     In in{cnt, idx, val};
-#define TD(T, SS) to_dense_kernel<T, SS><<<g, b, 0, s>>>(in, N, nx, ny, nz, (T *)phi)
+#define TD(T, SS) to_dense_kernel<T, SS><<<g, b, 0, s>>>(in, N, nx, ny, nz, (uint32_t)((int64_t)nx * ny * nz), 0u, (T *)phi)
     if (phi_dtype == MPF3D_F32) {
         if (slots == 4) TD(float, 4); else if (slots == 8) TD(float, 8); else if (slots == 16) TD(float, 16);
         else return MPF3D_ERR_ARG;
@@ -860,6 +1065,10 @@ extern "C" int mpf3d_compact_step(const uint32_t *cnt, const uint16_t *idx, cons
     P.use_torque = enable_anisotropy != 0 && enable_torque != 0;
     P.cells32 = (uint32_t)P.cells;
     P.sym_normals = symmetric_normals != 0;
+    P.base = 0;
+    P.n111_base = 0;
+    P.t_uniform = 0;
+    P.dT_uniform = 0.0f;
     {
         // a(0) and b(0): the values for a gradient below g2_floor
         const double pp = v[MPF3D_S_P_ROUND] * v[MPF3D_S_P_ROUND];
@@ -885,6 +1094,164 @@ extern "C" int mpf3d_compact_step(const uint32_t *cnt, const uint16_t *idx, cons
     if (slots == 4 && amax == 8) launch_step<4, 8>(in, out, M, P, Q, parity, err, s);
     else if (slots == 8 && amax == 16) launch_step<8, 16>(in, out, M, P, Q, parity, err, s);
     else if (slots == 16 && amax == 32) launch_step<16, 32>(in, out, M, P, Q, parity, err, s);
+    else return MPF3D_ERR_ARG;
+    return cudaGetLastError() == cudaSuccess ? MPF3D_OK : MPF3D_ERR_CUDA;
+}
+
+extern "C" int mpf3d_compact_to_dense_view(const uint32_t *head, const uint16_t *idx, const float *val, int slots,
+                                           uint32_t stride, uint32_t base, int N, int nx, int ny, int nz, void *phi,
+                                           int phi_dtype, void *stream) {
+    if (!phi || !head || !idx || !val || N <= 0 || N > 65535 || !dims_ok(nx, ny, nz)) return MPF3D_ERR_ARG;
+    if ((uint64_t)base + (uint64_t)nx * ny * nz > (uint64_t)stride) return MPF3D_ERR_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    dim3 b(32, 4, 2);
+    dim3 g = zfast_grid(nx, ny, nz, b);
+    In in{head, idx, val};
+#define TDV(T, SS) to_dense_kernel<T, SS><<<g, b, 0, s>>>(in, N, nx, ny, nz, stride, base, (T *)phi)
+    if (phi_dtype == MPF3D_F32) {
+        if (slots == 4) TDV(float, 4); else if (slots == 8) TDV(float, 8); else if (slots == 16) TDV(float, 16);
+        else return MPF3D_ERR_ARG;
+    } else if (phi_dtype == MPF3D_F64) {
+        if (slots == 4) TDV(double, 4); else if (slots == 8) TDV(double, 8); else if (slots == 16) TDV(double, 16);
+        else return MPF3D_ERR_ARG;
+    } else {
+        return MPF3D_ERR_DTYPE;
+    }
+#undef TDV
+    return cudaGetLastError() == cudaSuccess ? MPF3D_OK : MPF3D_ERR_CUDA;
+}
+
+namespace {
+
+// physics shared by every cell of a step, from the 13 kernel scalars
+Params shared_params(const mpf3d_scalars *sc, int enable_anisotropy, int enable_torque, int symmetric_normals) {
+    const double *v = sc->v;
+    Params P;
+    memset(&P, 0, sizeof P);
+    const double dx = v[MPF3D_S_DX];
+    P.inv_dx2 = (float)(1.0 / (dx * dx));
+    P.inv_2dx = (float)(1.0 / (2.0 * dx));
+    P.half_over_dx = (float)(0.5 / dx);
+    P.inv_dx = (float)(1.0 / dx);
+    P.dt = (float)v[MPF3D_S_DT];
+    P.eps0 = (float)v[MPF3D_S_EPS0_SL];
+    P.eps0sq = (float)(v[MPF3D_S_EPS0_SL] * v[MPF3D_S_EPS0_SL]);
+    P.w0 = (float)v[MPF3D_S_W0_SL];
+    P.mu_a = (float)v[MPF3D_S_MU_A];
+    P.delta_a = (float)v[MPF3D_S_DELTA_A];
+    P.mu_da = (float)(v[MPF3D_S_MU_A] * v[MPF3D_S_DELTA_A]);
+    P.pp = (float)(v[MPF3D_S_P_ROUND] * v[MPF3D_S_P_ROUND]);
+    P.tan_a0 = (float)tan(v[MPF3D_S_A0]);
+    P.g2_floor = (float)v[MPF3D_S_G2_FLOOR];
+    P.ksi = (float)v[MPF3D_S_KSI];
+    P.theta_c = (float)v[MPF3D_S_THETA_C_RAD];
+    P.Sf = (float)v[MPF3D_S_SF];
+    P.Tmc = v[MPF3D_S_T_MELT];
+    P.use_aniso = enable_anisotropy != 0;
+    P.use_torque = enable_anisotropy != 0 && enable_torque != 0;
+    P.sym_normals = symmetric_normals != 0;
+    const double pp = v[MPF3D_S_P_ROUND] * v[MPF3D_S_P_ROUND];
+    const double th = acos(0.0), thc = v[MPF3D_S_THETA_C_RAD];
+    double b = 1.0;
+    if (th < thc) {
+        double y = 0.5 * 3.14159265358979323846 * (th / thc);
+        y = fmin(fmax(y, 1e-6), 0.5 * 3.14159265358979323846 - 1e-6);
+        const double t = tan(y);
+        b = v[MPF3D_S_KSI] + (1.0 - v[MPF3D_S_KSI]) * t * tanh(1.0 / t);
+    }
+    P.b_flat = (float)b;
+    const double a_flat =
+        v[MPF3D_S_MU_A] * (1.0 + v[MPF3D_S_DELTA_A] * (sqrt(pp) + tan(v[MPF3D_S_A0]) * sqrt(1.0 + pp)));
+    const double e = v[MPF3D_S_EPS0_SL] * a_flat;
+    P.e2_flat = (float)(e * e);
+    return P;
+}
+
+int sms_of_current_device() {
+    int dev = 0, sms = 148;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    return sms;
+}
+
+template <int S, int AMAX>
+void launch_batched(const In &in, const Out &out, const Mats &M, const Params &P0, const mpf3d_instance *inst,
+                    int n_inst, int n_tiles, const Queue &Q, int parity, int32_t *err, cudaStream_t s) {
+    batched_sweep_kernel<S, AMAX><<<n_tiles, dim3(32, 8, 1), 0, s>>>(in, out, P0, inst, n_inst, Q, parity);
+    const int sms = sms_of_current_device();
+    batched_queue_kernel<S, AMAX, false><<<sms * 8, 256, 0, s>>>(in, out, M, P0, inst, n_inst, Q, parity, err);
+    if (P0.use_aniso)
+        batched_queue_kernel<S, AMAX, true><<<sms * 8, 128, 0, s>>>(in, out, M, P0, inst, n_inst, Q, parity, err);
+}
+
+}  // namespace
+
+extern "C" int mpf3d_batched_init_bicrystal(const mpf3d_instance *inst, int n_inst, uint32_t total_cells, double dx,
+                                            double delta, uint32_t *head, uint16_t *idx, float *val, int32_t *err,
+                                            void *stream) {
+    if (!inst || n_inst <= 0 || n_inst > 65535 || !head || !idx || !val || !err || total_cells == 0)
+        return MPF3D_ERR_ARG;
+    const float factor_dz = (float)((double)(float)(2.2 / delta) * dx);
+    Out o{head, idx, val};
+    batched_init_bicrystal_kernel<<<dim3(64, n_inst), 256, 0, (cudaStream_t)stream>>>(o, inst, n_inst, total_cells,
+                                                                                      factor_dz, err);
+    return cudaGetLastError() == cudaSuccess ? MPF3D_OK : MPF3D_ERR_CUDA;
+}
+
+extern "C" int mpf3d_batched_step(const uint32_t *head, const uint16_t *idx, const float *val, uint32_t *head_out,
+                                  uint16_t *idx_out, float *val_out, int slots, int amax, const mpf3d_instance *inst,
+                                  int n_inst, int n_tiles, uint32_t total_cells, const float *wij, const float *a2ij,
+                                  const float *mij, const float *n111, int N, const mpf3d_scalars *sc,
+                                  int enable_anisotropy, int enable_torque, int symmetric_normals,
+                                  uint32_t *work_items, uint32_t *work_count, int parity, int32_t *err,
+                                  void *stream) {
+    if (!head || !idx || !val || !head_out || !idx_out || !val_out || !inst || !wij || !a2ij || !mij || !n111 ||
+        !sc || !err || !work_items || !work_count || n_inst <= 0 || n_tiles <= 0 || total_cells == 0 || N <= 0 ||
+        N > 65535)
+        return MPF3D_ERR_ARG;
+    if (total_cells >= (1u << 31)) return MPF3D_ERR_TOO_LARGE;
+    if (head == head_out || idx == idx_out || val == val_out) return MPF3D_ERR_ARG;
+    Params P0 = shared_params(sc, enable_anisotropy, enable_torque, symmetric_normals);
+    P0.cells = total_cells;
+    P0.cells32 = total_cells;
+    P0.N = N;
+    In in{head, idx, val};
+    Out out{head_out, idx_out, val_out};
+    Mats M{nullptr, wij, a2ij, mij, n111};
+    Queue Q{work_items, work_count};
+    cudaStream_t s = (cudaStream_t)stream;
+    parity &= 1;
+    if (slots == 4 && amax == 8) launch_batched<4, 8>(in, out, M, P0, inst, n_inst, n_tiles, Q, parity, err, s);
+    else if (slots == 8 && amax == 16) launch_batched<8, 16>(in, out, M, P0, inst, n_inst, n_tiles, Q, parity, err, s);
+    else if (slots == 16 && amax == 32) launch_batched<16, 32>(in, out, M, P0, inst, n_inst, n_tiles, Q, parity, err, s);
+    else return MPF3D_ERR_ARG;
+    return cudaGetLastError() == cudaSuccess ? MPF3D_OK : MPF3D_ERR_CUDA;
+}
+
+extern "C" int mpf3d_batched_fronts(const uint32_t *head, const uint16_t *idx, const float *val, int slots,
+                                    const mpf3d_instance *inst, int n_inst, uint32_t total_cells, double *acc,
+                                    void *stream) {
+    if (!head || !idx || !val || !inst || !acc || n_inst <= 0 || n_inst > 65535) return MPF3D_ERR_ARG;
+    In in{head, idx, val};
+    dim3 g(16, n_inst);
+    cudaStream_t s = (cudaStream_t)stream;
+    if (slots == 4) batched_fronts_kernel<4><<<g, 256, 0, s>>>(in, inst, n_inst, total_cells, acc);
+    else if (slots == 8) batched_fronts_kernel<8><<<g, 256, 0, s>>>(in, inst, n_inst, total_cells, acc);
+    else if (slots == 16) batched_fronts_kernel<16><<<g, 256, 0, s>>>(in, inst, n_inst, total_cells, acc);
+    else return MPF3D_ERR_ARG;
+    return cudaGetLastError() == cudaSuccess ? MPF3D_OK : MPF3D_ERR_CUDA;
+}
+
+extern "C" int mpf3d_batched_gb_rows(const uint32_t *head, const uint16_t *idx, const float *val, int slots,
+                                     const mpf3d_instance *inst, int n_inst, uint32_t total_cells,
+                                     const int32_t *row_base, double *gb, void *stream) {
+    if (!head || !idx || !val || !inst || !row_base || !gb || n_inst <= 0 || n_inst > 65535) return MPF3D_ERR_ARG;
+    In in{head, idx, val};
+    dim3 g(16, n_inst);
+    cudaStream_t s = (cudaStream_t)stream;
+    if (slots == 4) batched_gb_rows_kernel<4><<<g, 128, 0, s>>>(in, inst, n_inst, total_cells, row_base, gb);
+    else if (slots == 8) batched_gb_rows_kernel<8><<<g, 128, 0, s>>>(in, inst, n_inst, total_cells, row_base, gb);
+    else if (slots == 16) batched_gb_rows_kernel<16><<<g, 128, 0, s>>>(in, inst, n_inst, total_cells, row_base, gb);
     else return MPF3D_ERR_ARG;
     return cudaGetLastError() == cudaSuccess ? MPF3D_OK : MPF3D_ERR_CUDA;
 }

@@ -45,6 +45,14 @@ _SIGS = {
     "mpf3d_compact_step": (_I32, [_VP, _VP, _VP, _VP, _VP, _VP, _I32, _I32, _VP, _F64, _VP, _VP, _VP, _VP,
                                   _I32, _I32, _I32, _I32, ctypes.POINTER(Scalars), _I32, _I32, _I32,
                                   _VP, _VP, _I32, _VP, _VP]),
+    "mpf3d_compact_to_dense_view": (_I32, [_VP, _VP, _VP, _I32, ctypes.c_uint32, ctypes.c_uint32, _I32, _I32,
+                                           _I32, _I32, _VP, _I32, _VP]),
+    "mpf3d_batched_init_bicrystal": (_I32, [_VP, _I32, ctypes.c_uint32, _F64, _F64, _VP, _VP, _VP, _VP, _VP]),
+    "mpf3d_batched_step": (_I32, [_VP, _VP, _VP, _VP, _VP, _VP, _I32, _I32, _VP, _I32, _I32, ctypes.c_uint32,
+                                  _VP, _VP, _VP, _VP, _I32, ctypes.POINTER(Scalars), _I32, _I32, _I32, _VP,
+                                  _VP, _I32, _VP, _VP]),
+    "mpf3d_batched_fronts": (_I32, [_VP, _VP, _VP, _I32, _VP, _I32, ctypes.c_uint32, _VP, _VP]),
+    "mpf3d_batched_gb_rows": (_I32, [_VP, _VP, _VP, _I32, _VP, _I32, ctypes.c_uint32, _VP, _VP, _VP]),
     "mpf3d_compact_step_noalloc": (_I32, [_VP, _VP, _VP, _VP, _VP, _VP, _I32, _I32, _VP, _F64, _VP, _VP,
                                           _VP, _VP, _I32, _I32, _I32, _I32, ctypes.POINTER(Scalars),
                                           _I32, _I32, _I32, _VP, _VP]),
