@@ -298,8 +298,17 @@ def run_ours(args, rank, world):
         cpu = {"value": v, "unit": UNIT, "cores": th, "kind": "port",
                "sample": f"64x64x256 crop of the workload (N=65), {st} oracle steps (reference "
                          f"float32 typing), OpenMP"}
+    extra = {}
+    if rank == 0 and not args.no_accuracy and args.accuracy_steps > 0:
+        del solver
+        torch.cuda.empty_cache()
+        extra["accuracy_fp32_vs_fp64"] = accuracy_run(args, phi0, temp, n111, wij, aij, mij, phys, dev)
+    del phi0
+    torch.cuda.empty_cache()
+    if rank == 0 and not args.no_bicrystal and args.bicrystal_steps > 0:
+        extra["bicrystal_batch"] = bicrystal_run(args, dev)
     emit(args, rank, world, value, ms, cells, t_e2e, in_bytes, out_bytes, achieved, peak, peak_kind,
-         traffic, bytes_per_launch, occ, clk, cpu, final_cnt_sum)
+         traffic, bytes_per_launch, occ, clk, cpu, final_cnt_sum, extra)
 
 
 def e2e_run(args, phi0, temp, n111, wij, aij, mij, phys, dev, barrier, world):
@@ -327,8 +336,106 @@ def e2e_run(args, phi0, temp, n111, wij, aij, mij, phys, dev, barrier, world):
     return t_e2e, in_bytes, out_bytes
 
 
+def interface_height(phi_liquid):
+    """Mean over columns of the highest z with solid fraction > 0.5
+    (interface_positions_3d, tests/verification_3d.py:409-416)."""
+    import torch
+    solid = 1.0 - phi_liquid
+    mask = solid > 0.5
+    nz = mask.shape[-1]
+    ks = torch.arange(nz, device=mask.device).view(1, 1, nz)
+    top = torch.where(mask, ks, torch.full_like(ks, -1)).amax(dim=-1)
+    ok = top >= 0
+    return float(top[ok].double().mean().item()) if bool(ok.any()) else float("nan")
+
+
+def accuracy_run(args, phi0, temp, n111, wij, aij, mij, phys, dev):
+    """The same workload in FP64 with the reference's numerics (dense drop-in
+    kernels, float64 phi, temperature and scalars) and in the FP32 compact
+    form; reports max|dphi|, mean interface height and grain volume
+    fractions of both after the same number of steps."""
+    import torch
+    from mpf3d.solver import CompactSolver
+    from src import gpu_kernels_3d as K
+    steps = args.accuracy_steps
+    N, nx, ny, nz = phi0.shape
+    rate = phys.derived()["cooling_rate"]
+    t0 = time.perf_counter()
+    c = CompactSolver(phi0, temp, n111, wij, aij, mij, phys, slots=args.slots)
+    c.step(steps)
+    p32 = c.to_dense(host=False).double()
+    del c
+    torch.cuda.empty_cache()
+    t32 = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    p = phi0.double().contiguous()
+    q = torch.empty_like(p)
+    T = torch.from_numpy(np.broadcast_to(np.asarray(temp, np.float64), (nx, ny, nz)).copy()).to(dev)
+    mf = torch.zeros((50, nx, ny, nz), dtype=torch.int32, device=dev)
+    nf = torch.zeros((nx, ny, nz), dtype=torch.int32, device=dev)
+    W, A, M, U = (torch.from_numpy(np.ascontiguousarray(a)).to(dev) for a in (wij, aij, mij, n111))
+    sc = phys.kernel_scalars(f32=False)
+    cfg = ((1, 1, 1), (4, 4, 4))
+    for _ in range(steps):
+        K.kernel_update_temp_3d[cfg](T, np.float64(rate), nx, ny, nz)
+        K.kernel_update_nfmf_3d[cfg](p, mf, nf, nx, ny, nz, N)
+        K.kernel_update_phasefield_active_3d[cfg](p, q, T, mf, nf, W, A, M, U, nx, ny, nz, N, *sc)
+        p, q = q, p
+    torch.cuda.synchronize(dev)
+    K.check_errors()
+    t64 = time.perf_counter() - t0
+    cells = nx * ny * nz
+    vf64 = (p[1:].sum(dim=(1, 2, 3)) / cells).cpu().numpy()
+    vf32 = (p32[1:].sum(dim=(1, 2, 3)) / cells).cpu().numpy()
+    out = {"steps": steps, "grid": [nx, ny, nz], "phases": N,
+           "max_abs_dphi": float((p - p32).abs().max().item()),
+           "interface_height_cells": {"fp64": interface_height(p[0]), "fp32": interface_height(p32[0])},
+           "grain_volume_fraction_max_abs_diff": float(np.abs(vf64 - vf32).max()),
+           "solid_fraction": {"fp64": float(vf64.sum()), "fp32": float(vf32.sum())},
+           "seconds": {"fp32_compact": t32, "fp64_dense_reference_numerics": t64},
+           "tolerance": 1e-4}
+    out["within_tolerance"] = out["max_abs_dphi"] <= 1e-4
+    del p, q, p32, mf
+    torch.cuda.empty_cache()
+    return out
+
+
+def bicrystal_run(args, dev):
+    """Batched bicrystals: 512 instances of sizes drawn from {64,96,128}^2 x
+    {64,96}, undercooling U[0.25, 3] K, anisotropy strength U[0, 1], random
+    orientation pairs, stepped together from CUDA-graph replays; outputs
+    velocity ratio and grain-boundary inclination per instance."""
+    import torch
+    from mpf3d.batched import BatchedBicrystals, sample_batch
+    n = args.bicrystal_instances
+    dims, q, dT, da = sample_batch(n, seed=SEED)
+    b = BatchedBicrystals(dims, q, dT, da, base_height=16.0, slots=4, device=dev)
+    b.capture(50)
+    b.step(50)  # warm-up replay
+    torch.cuda.synchronize(dev)
+    b = BatchedBicrystals(dims, q, dT, da, base_height=16.0, slots=4, device=dev)
+    b.capture(50)
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    res = b.run(args.bicrystal_steps, sample_every=100, graph_steps=50)
+    torch.cuda.synchronize(dev)
+    wall = time.perf_counter() - t0
+    ratio = res["velocity_ratio"]
+    ang = res["gb_angle_deg"]
+    fin = np.isfinite(ratio)
+    return {"instances": n, "steps": args.bicrystal_steps, "cells_per_step": b.total_cells,
+            "wall_s": wall, "cases_per_hour": n / wall * 3600.0,
+            "cell_steps_per_s": b.total_cells * args.bicrystal_steps / wall,
+            "velocity_ratio": {"finite": int(fin.sum()),
+                               "median": float(np.median(ratio[fin])) if fin.any() else None},
+            "gb_inclination_deg": {"finite": int(np.isfinite(ang).sum()),
+                                   "median_abs": float(np.nanmedian(np.abs(ang))) if np.isfinite(ang).any()
+                                   else None},
+            "launches_per_step": 3, "graph_steps": 50}
+
+
 def emit(args, rank, world, value, ms, cells, t_e2e, in_bytes, out_bytes, achieved, peak, peak_kind,
-         traffic, bytes_per_launch, occ, clk, cpu, final_cnt_sum):
+         traffic, bytes_per_launch, occ, clk, cpu, final_cnt_sum, extra=None):
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
@@ -337,7 +444,7 @@ def emit(args, rank, world, value, ms, cells, t_e2e, in_bytes, out_bytes, achiev
                 "e2e": {"value": cells * args.steps * world / t_e2e, "unit": UNIT,
                         "h2d_bytes_per_step": in_bytes / args.steps,
                         "d2h_bytes_per_step": out_bytes / args.steps},
-                "gpu_launches": args.steps,
+                "gpu_launches": 3 * args.steps,
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                              "frac": achieved / peak, "traffic": traffic,
                              "peak_source": peak_kind,
@@ -346,8 +453,56 @@ def emit(args, rank, world, value, ms, cells, t_e2e, in_bytes, out_bytes, achiev
                 "stored_phases_per_cell": {"start": occ[0] / cells, "end": occ[-1] / cells},
                 "clocks": clk.summary(),
                 "cpu_baseline": cpu}
+        line.update(extra or {})
         assert final_cnt_sum == occ[-1], "timed and accounting runs diverged"
         print(json.dumps(line), flush=True)
+
+
+def run_c3(args):
+    """Large single domain in FP32: 1024 x 1024 x 256 cells, 512 grains seeded
+    in the bottom 24 layers + liquid (N = 513), started directly in compact
+    form from the owner map (the dense field would need 551 GB)."""
+    import torch
+    from mpf3d import inputs
+    from mpf3d.solver import CompactSolver
+    dev = torch.device("cuda:0")
+    nx, ny, nz, ng, slab = 1024, 1024, 256, 512, 24
+    phys = inputs.Physics()
+    d = phys.derived()
+    t0 = time.perf_counter()
+    owner = inputs.voronoi_slab_owner(nx, ny, slab, ng, slab, SEED)
+    prof = inputs.tanh_profile(nz, slab, phys.dx, d["delta"])
+    temp = inputs.temperature_field(1, 1, nz, phys.T_melt, phys.G, phys.dx, slab)[0, 0]
+    q = inputs.random_quaternions(ng, ORIENT_SEED)
+    wij, aij, mij = inputs.matrices_for(phys, ng + 1)
+    n111 = inputs.rotated_n111(q)
+    s = CompactSolver.from_owner(owner, prof, temp, n111, wij, aij, mij, phys, slots=args.slots)
+    setup = time.perf_counter() - t0
+    s.step(args.warmup)
+    torch.cuda.synchronize(dev)
+    stream = torch.cuda.current_stream(dev)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(0) as clk:
+        torch.cuda.synchronize(dev)
+        e0.record(stream)
+        for i in range(args.steps):
+            s.launch_step(args.warmup + i + 1)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+    s.check()
+    ms = e0.elapsed_time(e1)
+    cells = nx * ny * nz
+    line = {"metric": "3D cell-steps/s (FP32 compact step, 1024x1024x256, N=513)",
+            "value": cells * args.steps / (ms / 1e3), "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+            "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "1024x1024x256, 512 grains in the bottom 24 layers + liquid (N=513), "
+                                   "anisotropy+torque, uniform cooling, FP32 compact, started from the owner map",
+                       "slots": s.slots, "state_bytes_per_buffer": s.state_bytes()},
+            "setup_s": setup, "stored_phases_per_cell_end": float(s.stored_counts().double().mean().item()),
+            "clocks": clk.summary(), "gpu_launches": 3 * args.steps}
+    print(json.dumps(line), flush=True)
 
 
 def main():
@@ -356,11 +511,18 @@ def main():
     ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="c2", choices=["c2", "c3"],
+                    help="c2: the 256^3 bench line; c3: the 1024x1024x256 large-domain run")
     ap.add_argument("--slots", type=int, default=16)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end run (profiling)")
     ap.add_argument("--grid", type=int, nargs=3, default=None,
                     help="override the 256^3 grid (smaller cases for profiling)")
+    ap.add_argument("--accuracy-steps", type=int, default=2000)
+    ap.add_argument("--no-accuracy", action="store_true")
+    ap.add_argument("--bicrystal-steps", type=int, default=3000)
+    ap.add_argument("--bicrystal-instances", type=int, default=512)
+    ap.add_argument("--no-bicrystal", action="store_true")
     args = ap.parse_args()
     global GRID
     if args.grid:
@@ -374,6 +536,8 @@ def main():
         torch.distributed.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     if args.impl == "reference":
         run_reference(args, rank)
+    elif args.workload == "c3":
+        run_c3(args)
     else:
         run_ours(args, rank, world)
     if world > 1 and args.impl == "ours":

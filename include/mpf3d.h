@@ -105,6 +105,16 @@ int mpf3d_compact_from_dense(const void *phi, int phi_dtype, int N, int nx, int 
 int mpf3d_compact_to_dense(const uint32_t *head, const uint16_t *idx, const float *val, int slots, int N,
                            int nx, int ny, int nz, void *phi, int phi_dtype, void *stream);
 
+/* Initial state from a grain-owner map and a z profile (the 3-D analogue of
+ * init_phi_from_grain_map_3d, src/seed_modes_3d.py:38-57): owner int32
+ * [slab][ny][nx] (x fastest) gives the grain of the first `slab` layers,
+ * higher layers repeat layer slab-1; the grain holds prof[k] (float [nz]),
+ * the liquid clip(1 - prof[k], 0, 1).  No dense phi is formed, so domains
+ * whose dense field would not fit (e.g. 1024 x 1024 x 256 with 513 phases)
+ * start directly in compact form. */
+int mpf3d_compact_init_owner(const int32_t *owner, int slab, const float *prof, int nx, int ny, int nz,
+                             int slots, uint32_t *head, uint16_t *idx, float *val, void *stream);
+
 /* nf of the reference's APT (kernel_update_nfmf_3d, src/gpu_kernels_3d.py:462-486)
  * computed from a compact state, dense z-fastest int32 output. */
 int mpf3d_compact_active_count(const uint32_t *head, const uint16_t *idx, int slots, int nx, int ny, int nz,

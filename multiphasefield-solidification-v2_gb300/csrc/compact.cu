@@ -937,6 +937,33 @@ __global__ void batched_gb_rows_kernel(In in, const mpf3d_instance *__restrict__
     }
 }
 
+
+// Initial state from a grain-owner map and a z profile: owner[k][m][l]
+// (x fastest) holds the grain of the first `slab` layers; rows above the slab
+// repeat the top layer.  The grain holds prof[k], the liquid
+// clip(1 - prof[k], 0, 1) (init_phi_from_grain_map_3d,
+// src/seed_modes_3d.py:38-57, with a 3-D owner map).
+__global__ void init_owner_kernel(Out out, const int32_t *__restrict__ owner, int slab, const float *__restrict__ prof,
+                                  int nx, int ny, int nz, uint32_t cells) {
+    const uint32_t plane = (uint32_t)nx * (uint32_t)ny;
+    for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < cells; c += gridDim.x * blockDim.x) {
+        const int k = (int)(c / plane);
+        const uint32_t col = c - (uint32_t)k * plane;
+        const int g = owner[(uint32_t)min(k, slab - 1) * plane + col];
+        const float s = prof[k];
+        const float liq = fminf(fmaxf(1.0f - s, 0.0f), 1.0f);
+        int n = 0, id0 = 0;
+        float v0 = 0.0f;
+        if (liq > 0.0f) { id0 = LIQ; v0 = liq; out.val[c] = liq; n = 1; }
+        if (s > 0.0f) {
+            if (n == 0) { id0 = g; v0 = s; out.val[c] = s; }
+            else { out.idx[(size_t)cells + c] = (uint16_t)g; out.val[(size_t)cells + c] = s; }
+            ++n;
+        }
+        out.head[c] = mkhead(id0, n, n == 1 && v0 != 1.0f);
+    }
+}
+
 }  // namespace compact
 }  // namespace mpf3d
 
@@ -1253,6 +1280,18 @@ extern "C" int mpf3d_batched_gb_rows(const uint32_t *head, const uint16_t *idx, 
     else if (slots == 8) batched_gb_rows_kernel<8><<<g, 128, 0, s>>>(in, inst, n_inst, total_cells, row_base, gb);
     else if (slots == 16) batched_gb_rows_kernel<16><<<g, 128, 0, s>>>(in, inst, n_inst, total_cells, row_base, gb);
     else return MPF3D_ERR_ARG;
+    return cudaGetLastError() == cudaSuccess ? MPF3D_OK : MPF3D_ERR_CUDA;
+}
+
+extern "C" int mpf3d_compact_init_owner(const int32_t *owner, int slab, const float *prof, int nx, int ny, int nz,
+                                        int slots, uint32_t *head, uint16_t *idx, float *val, void *stream) {
+    if (!owner || !prof || !head || !idx || !val || slab <= 0 || slab > nz || slots < 2 || !dims_ok(nx, ny, nz))
+        return MPF3D_ERR_ARG;
+    const int64_t cells = (int64_t)nx * ny * nz;
+    if (cells >= ((int64_t)1 << 32)) return MPF3D_ERR_TOO_LARGE;
+    Out o{head, idx, val};
+    init_owner_kernel<<<sms_of_current_device() * 16, 256, 0, (cudaStream_t)stream>>>(o, owner, slab, prof, nx, ny, nz,
+                                                                                       (uint32_t)cells);
     return cudaGetLastError() == cudaSuccess ? MPF3D_OK : MPF3D_ERR_CUDA;
 }
 

@@ -155,7 +155,7 @@ def voronoi_slab_owner(nx, ny, nz, n_grains, slab, seed) -> np.ndarray:
     tree = cKDTree(np.stack([sx, sy, sz], 1) % [nx, ny, big], boxsize=[nx, ny, big])
     ks = min(slab, nz)
     gx, gy, gz = np.meshgrid(np.arange(nx), np.arange(ny), np.arange(ks), indexing="ij")
-    _, idx = tree.query(np.stack([gx.ravel(), gy.ravel(), gz.ravel()], 1).astype(np.float64))
+    _, idx = tree.query(np.stack([gx.ravel(), gy.ravel(), gz.ravel()], 1).astype(np.float64), workers=-1)
     owner = np.empty((nx, ny, nz), np.int32)
     owner[:, :, :ks] = (idx.reshape(nx, ny, ks) + 1).astype(np.int32)
     if nz > ks:

@@ -22,6 +22,13 @@ from .inputs import Physics
 _SLOT_TEMPLATES = {4: 8, 8: 16, 16: 32}  # slots -> max active phases per cell
 
 
+class _DenseShape:
+    """Shape-only stand-in for a dense phi that is never formed."""
+
+    def __init__(self, N, nx, ny, nz):
+        self.shape = (N, nx, ny, nz)
+
+
 class SlotOverflow(RuntimeError):
     """A cell needed more slots (or active phases) than the template holds."""
 
@@ -60,12 +67,19 @@ def z_profile(temp) -> np.ndarray:
 
 
 class CompactSolver:
+    """Compact FP32 stepper of one domain.  Build it from a dense phi0 or, for
+    domains whose dense field does not fit, with `from_owner`."""
+
     def __init__(self, phi0, temp0, n111, wij, aij, mij, phys: Physics | None = None, *,
                  scalars=None, T_melt=None, cooling_rate=None, slots: int = 8,
                  anisotropy: bool = True, torque: bool = True, device="cuda:0"):
         torch = _torch()
         if slots not in _SLOT_TEMPLATES:
             raise ValueError(f"slots must be one of {sorted(_SLOT_TEMPLATES)}")
+        owner_init = None
+        if isinstance(phi0, tuple) and len(phi0) == 3 and phi0[0] == "owner":
+            owner_init = phi0[1]
+            phi0 = _DenseShape(*phi0[2])
         self.phys = phys or Physics()
         d = self.phys.derived()
         self.scalars = _scalars_from(scalars if scalars is not None else self.phys)
@@ -73,9 +87,12 @@ class CompactSolver:
         self.cooling_rate = float(d["cooling_rate"] if cooling_rate is None else cooling_rate)
         self.anisotropy, self.torque = bool(anisotropy), bool(torque)
         self.device = torch.device(device)
-        phi = phi0 if isinstance(phi0, torch.Tensor) else torch.from_numpy(np.ascontiguousarray(phi0))
-        if phi.dim() != 4 or phi.dtype not in (torch.float32, torch.float64):
-            raise ValueError("phi0 must be float32/float64 [N, nx, ny, nz]")
+        if owner_init is not None:
+            phi = phi0
+        else:
+            phi = phi0 if isinstance(phi0, torch.Tensor) else torch.from_numpy(np.ascontiguousarray(phi0))
+            if phi.dim() != 4 or phi.dtype not in (torch.float32, torch.float64):
+                raise ValueError("phi0 must be float32/float64 [N, nx, ny, nz]")
         self.N, self.nx, self.ny, self.nz = (int(s) for s in phi.shape)
         self.cells = self.nx * self.ny * self.nz
         self.slots = slots
@@ -102,9 +119,32 @@ class CompactSolver:
         self.buf = [self._alloc(), self._alloc()]
         self.cur = 0
         self.step_count = 0
-        dphi = phi.to(self.device).contiguous()
-        self._from_dense(dphi)
+        if owner_init is not None:
+            owner, slab, prof = owner_init
+            h, i_, v = self.buf[0]
+            rc = _lib.lib().mpf3d_compact_init_owner(owner.data_ptr(), slab, prof.data_ptr(), self.nx, self.ny,
+                                                     self.nz, self.slots, h.data_ptr(), i_.data_ptr(),
+                                                     v.data_ptr(), self._stream())
+            _lib.check(rc, "compact_init_owner")
+        else:
+            dphi = phi.to(self.device).contiguous()
+            self._from_dense(dphi)
         self.check()
+
+    @classmethod
+    def from_owner(cls, owner, profile, temp0, n111, wij, aij, mij, phys: Physics | None = None, **kw):
+        """Start from a grain-owner map of the first `slab` z-layers (int32
+        [nx, ny, slab], grains 1..N-1; higher layers repeat the top one) and a
+        solid-fraction z profile, without forming the dense field."""
+        torch = _torch()
+        own = np.asarray(owner)
+        nx, ny, slab = own.shape
+        nz = len(profile)
+        N = int(np.asarray(wij).shape[0])
+        dev = torch.device(kw.get("device", "cuda:0"))
+        o = torch.as_tensor(np.ascontiguousarray(own.transpose(2, 1, 0)), dtype=torch.int32).to(dev)
+        p = torch.as_tensor(np.ascontiguousarray(profile, np.float32)).to(dev)
+        return cls(("owner", (o, slab, p), (N, nx, ny, nz)), temp0, n111, wij, aij, mij, phys, **kw)
 
     # -- buffers ---------------------------------------------------------------
     def _alloc(self):

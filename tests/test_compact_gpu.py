@@ -88,3 +88,26 @@ def test_slot_template_widens_instead_of_dropping_phases():
     b = make_solver(case, slots=16)
     b.step(6)
     assert np.array_equal(a.to_dense(), b.to_dense())
+
+
+def test_owner_map_start_equals_dense_start():
+    """The owner-map initializer builds the same state as converting the
+    dense field of the same owner map and profile."""
+    from mpf3d import inputs
+    from mpf3d.solver import CompactSolver
+    phys = inputs.Physics()
+    d = phys.derived()
+    nx, ny, nz, n, slab = 24, 20, 30, 7, 8
+    owner = inputs.voronoi_slab_owner(nx, ny, nz, n, slab, seed=9)
+    prof = inputs.tanh_profile(nz, slab, phys.dx, d["delta"])
+    phi = inputs.phi_from_owner(owner, n, prof)
+    temp = inputs.temperature_field(nx, ny, nz, phys.T_melt, phys.G, phys.dx, slab)
+    q = inputs.random_quaternions(n, 4)
+    wij, aij, mij = inputs.matrices_for(phys, n + 1)
+    n111 = inputs.rotated_n111(q)
+    a = CompactSolver(phi, temp, n111, wij, aij, mij, phys)
+    b = CompactSolver.from_owner(owner[:, :, :slab], prof, temp, n111, wij, aij, mij, phys)
+    assert np.array_equal(a.to_dense(), b.to_dense())
+    a.step(3)
+    b.step(3)
+    assert np.array_equal(a.to_dense(), b.to_dense())
