@@ -373,7 +373,7 @@ def accuracy_run(args, phi0, temp, n111, wij, aij, mij, phys, dev):
         def __init__(self, dtype, f32):
             self.p = phi0.to(dtype=dtype, copy=True).contiguous()
             self.q = torch.empty_like(self.p)
-            self.T = torch.from_numpy(T0.astype(np.float32 if f32 else np.float64)).to(dev)
+            self.T = torch.from_numpy(np.ascontiguousarray(T0, dtype=np.float32 if f32 else np.float64)).to(dev)
             self.mf = torch.zeros((50, nx, ny, nz), dtype=torch.int32, device=dev)
             self.nf = torch.zeros((nx, ny, nz), dtype=torch.int32, device=dev)
             self.sc = phys.kernel_scalars(f32=f32)
