@@ -206,6 +206,38 @@ int mpf3d_batched_gb_rows(const uint32_t *head, const uint16_t *idx, const float
                           const mpf3d_instance *inst, int n_inst, uint32_t total_cells, const int32_t *row_base,
                           double *gb, void *stream);
 
+/* ---- surrogate network kernels (BF16 tensor cores, FP32 accumulate) ------
+ * No reference counterpart: the reference has no learned component.  BF16
+ * values are passed as uint16_t bit patterns. */
+
+/* C[m][n] = act(sum_k A(m,k) B(k,n) + bias[n]) with A(m,k) = A[m*sam + k*sak],
+ * B(k,n) = B[k*sbk + n*sbn]; act 0 = none, 1 = SiLU.  Z (nullable) receives
+ * the FP32 pre-activation, Y the result (BF16 if y_bf16, else FP32, added to
+ * Y when beta = 1), both with row stride ldy.  mma.sync m16n8k16 tiles. */
+int mpf3d_gemm_bf16(int M, int N, int K, const uint16_t *A, int64_t sam, int64_t sak, const uint16_t *B,
+                    int64_t sbk, int64_t sbn, const float *bias, int act, float *Z, void *Y, int ldy,
+                    int y_bf16, int beta, void *stream);
+
+/* dZ = dY * act'(Z) elementwise; outputs BF16 and/or FP32 (each nullable). */
+int mpf3d_act_backward(const float *dY, const float *Z, int act, int64_t n, uint16_t *dZ16, float *dZ32,
+                       void *stream);
+
+/* out[n] = sum over m of X[m*ld + n]. */
+int mpf3d_colsum(const float *X, int M, int N, int ld, float *out, void *stream);
+
+/* Weighted MSE of the first n_out columns of pred (row stride ld) against
+ * target [M][n_out]: *loss += sum w_c (pred - t)^2 / M, dpred = its gradient. */
+int mpf3d_mse(const float *pred, int ld, const float *target, int M, int n_out, const float *w, float *dpred,
+              float *loss, void *stream);
+
+/* Adam step `step` (1-based) on FP32 weights with decoupled weight decay
+ * folded into the gradient; w16 (nullable) receives the BF16 copy. */
+int mpf3d_adam(float *w, float *m, float *v, const float *g, uint16_t *w16, int64_t n, float lr, float b1,
+               float b2, float eps, int step, float weight_decay, void *stream);
+
+/* FP32 -> BF16, round to nearest even. */
+int mpf3d_f32_to_bf16(const float *x, uint16_t *y, int64_t n, void *stream);
+
 /* Largest grid (nx*ny*nz) that mpf3d_compact_step_noalloc accepts. */
 #define MPF3D_NOALLOC_MAX_CELLS 4194304u
 

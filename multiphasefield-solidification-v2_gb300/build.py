@@ -25,6 +25,7 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I" + INCLUD
 SOURCES = [
     ("dense_ref.cu", ["-fmad=false"]),
     ("compact.cu", []),
+    ("mlp.cu", []),
 ]
 
 

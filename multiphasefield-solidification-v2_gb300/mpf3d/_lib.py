@@ -54,6 +54,14 @@ _SIGS = {
     "mpf3d_batched_fronts": (_I32, [_VP, _VP, _VP, _I32, _VP, _I32, ctypes.c_uint32, _VP, _VP]),
     "mpf3d_batched_gb_rows": (_I32, [_VP, _VP, _VP, _I32, _VP, _I32, ctypes.c_uint32, _VP, _VP, _VP]),
     "mpf3d_compact_init_owner": (_I32, [_VP, _I32, _VP, _I32, _I32, _I32, _I32, _VP, _VP, _VP, _VP]),
+    "mpf3d_gemm_bf16": (_I32, [_I32, _I32, _I32, _VP, _I64, _I64, _VP, _I64, _I64, _VP, _I32, _VP, _VP, _I32,
+                               _I32, _I32, _VP]),
+    "mpf3d_act_backward": (_I32, [_VP, _VP, _I32, _I64, _VP, _VP, _VP]),
+    "mpf3d_colsum": (_I32, [_VP, _I32, _I32, _I32, _VP, _VP]),
+    "mpf3d_mse": (_I32, [_VP, _I32, _VP, _I32, _I32, _VP, _VP, _VP, _VP]),
+    "mpf3d_adam": (_I32, [_VP, _VP, _VP, _VP, _VP, _I64, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                          ctypes.c_float, _I32, ctypes.c_float, _VP]),
+    "mpf3d_f32_to_bf16": (_I32, [_VP, _VP, _I64, _VP]),
     "mpf3d_compact_step_noalloc": (_I32, [_VP, _VP, _VP, _VP, _VP, _VP, _I32, _I32, _VP, _F64, _VP, _VP,
                                           _VP, _VP, _I32, _I32, _I32, _I32, ctypes.POINTER(Scalars),
                                           _I32, _I32, _I32, _VP, _VP]),

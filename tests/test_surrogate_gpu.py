@@ -1,0 +1,125 @@
+"""Surrogate network kernels on the GPU: the BF16 tensor-core GEMM against a
+float64 product of the same BF16 operands (all operand layouts the network
+uses), the full backward pass against a CPU float64 restatement with the same
+BF16 rounding points, and training on a smooth target."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+
+def bf16_round(x):
+    """Round float values to BF16 (nearest even), returned as float64."""
+    u = np.asarray(x, np.float32).view(np.uint32).astype(np.uint64)
+    u = (u + 0x7FFF + ((u >> 16) & 1)) >> 16
+    return (u.astype(np.uint32) << 16).view(np.float32).astype(np.float64)
+
+
+def to_bf16_bits(x):
+    u = np.asarray(x, np.float32).view(np.uint32).astype(np.uint64)
+    return ((u + 0x7FFF + ((u >> 16) & 1)) >> 16).astype(np.uint16).view(np.int16)
+
+
+@pytest.mark.parametrize("M,N,K,transA,transB", [(100, 70, 40, False, False), (64, 256, 16, False, True),
+                                                 (256, 16, 300, True, False), (33, 2, 256, False, True)])
+def test_gemm_matches_float64(M, N, K, transA, transB):
+    from mpf3d import _lib
+    rng = np.random.default_rng(M + N + K)
+    A = rng.standard_normal((M, K)).astype(np.float32)
+    B = rng.standard_normal((K, N)).astype(np.float32)
+    bias = rng.standard_normal(N).astype(np.float32)
+    A_store = A.T.copy() if transA else A
+    B_store = B.T.copy() if transB else B
+    sam, sak = (1, M) if transA else (K, 1)
+    sbk, sbn = (1, K) if transB else (N, 1)
+    dev = torch.device("cuda:0")
+    tA = torch.from_numpy(to_bf16_bits(A_store)).to(dev)
+    tB = torch.from_numpy(to_bf16_bits(B_store)).to(dev)
+    tb = torch.from_numpy(bias).to(dev)
+    Y = torch.empty((M, N), dtype=torch.float32, device=dev)
+    Z = torch.empty((M, N), dtype=torch.float32, device=dev)
+    rc = _lib.lib().mpf3d_gemm_bf16(M, N, K, tA.data_ptr(), sam, sak, tB.data_ptr(), sbk, sbn, tb.data_ptr(), 1,
+                                    Z.data_ptr(), Y.data_ptr(), N, 0, 0, None)
+    assert rc == 0
+    ref_z = bf16_round(A) @ bf16_round(B) + bias
+    ref_y = ref_z / (1.0 + np.exp(-ref_z))
+    got_z = Z.cpu().numpy()
+    got_y = Y.cpu().numpy()
+    scale = np.abs(ref_z).max()
+    assert np.abs(got_z - ref_z).max() <= 1e-5 * scale * np.sqrt(K)
+    assert np.abs(got_y - ref_y).max() <= 1e-3 * scale
+
+
+def cpu_forward_backward(layers, X, target, w):
+    """Float64 restatement of Surrogate.forward/backward with the GPU's BF16
+    rounding points: hidden activations and the dZ operands of the GEMMs are
+    BF16, pre-activations and accumulations exact."""
+    silu = lambda z: z / (1.0 + np.exp(-z))
+    dsilu = lambda z: (1 / (1 + np.exp(-z))) * (1 + z * (1 - 1 / (1 + np.exp(-z))))
+    hs, zs = [X], []
+    h = X
+    for i, (W, b) in enumerate(layers):
+        z = h @ W.T + b
+        zs.append(z)
+        h = z if i == len(layers) - 1 else bf16_round(silu(z))
+        hs.append(h)
+    out = h
+    M = X.shape[0]
+    dY = 2.0 * w * (out - target) / M
+    grads = []
+    for i in range(len(layers) - 1, -1, -1):
+        W, b = layers[i]
+        dZ = dY if i == len(layers) - 1 else dY * dsilu(zs[i])
+        dZ16 = bf16_round(dZ)
+        grads.append((dZ16.T @ hs[i], dZ.sum(0)))
+        dY = dZ16 @ W
+    return out, grads[::-1]
+
+
+def test_backward_matches_cpu_float64_restatement():
+    from mpf3d.surrogate import Surrogate, LAYERS, IN_FEATURES, HIDDEN, K1
+    s = Surrogate(seed=3)
+    rng = np.random.default_rng(0)
+    M = 96
+    X = rng.uniform(-1, 1, (M, IN_FEATURES)).astype(np.float32)
+    T = rng.standard_normal((M, 2)).astype(np.float32)
+    x16 = s.prepare(X)
+    tT = torch.from_numpy(T).to("cuda:0")
+    s.loss_and_grad(x16, tT)
+    g = s.g.cpu().numpy().astype(np.float64)
+    layers = s.bf16_weights()
+    Xp = np.zeros((M, K1))
+    Xp[:, :IN_FEATURES] = bf16_round(X)
+    out, grads = cpu_forward_backward(layers, Xp, T.astype(np.float64), np.ones(2))
+    gpu_out = s.forward(x16).cpu().numpy()
+    assert np.abs(gpu_out - out).max() <= 2e-2 * max(1.0, np.abs(out).max())
+    for layer, (K, N, _) in enumerate(LAYERS):
+        o, ob = s.offsets[layer]
+        gW = g[o:o + N * K].reshape(N, K)
+        gb = g[ob:ob + N]
+        rW, rb = grads[layer]
+        if layer == 0:
+            rW = rW.copy()
+            rW[:, IN_FEATURES:] = 0.0
+        for got, ref in ((gW, rW), (gb, rb)):
+            err = np.linalg.norm(got - ref) / max(np.linalg.norm(ref), 1e-12)
+            assert err <= 2e-2, f"layer {layer}: relative gradient error {err:.3e}"
+
+
+def test_training_fits_a_smooth_target():
+    from mpf3d.surrogate import Surrogate
+    rng = np.random.default_rng(1)
+    n = 512
+    q1 = rng.standard_normal((n, 4))
+    q1 /= np.linalg.norm(q1, axis=1, keepdims=True)
+    q2 = rng.standard_normal((n, 4))
+    q2 /= np.linalg.norm(q2, axis=1, keepdims=True)
+    dT = rng.uniform(0.25, 3.0, n)
+    da = rng.uniform(0, 1, n)
+    y = np.stack([np.sin(2 * dT) + da, dT * da - 0.5], 1)
+    s = Surrogate(seed=0)
+    hist = s.fit(q1, q2, dT, da, y, epochs=150, batch=128, lr=3e-3, augment_symmetry=False)
+    assert hist[-1] < 0.05 * hist[0]
+    pred = s.predict(q1, q2, dT, da)
+    assert np.sqrt(np.mean((pred - y) ** 2)) < 0.1
