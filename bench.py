@@ -553,7 +553,7 @@ def main():
     ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "accuracy"],
+    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "accuracy", "c5"],
                     help="c2: the 256^3 bench line; c3: the 1024x1024x256 large-domain run")
     ap.add_argument("--slots", type=int, default=16)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -565,6 +565,8 @@ def main():
     ap.add_argument("--bicrystal-steps", type=int, default=3000)
     ap.add_argument("--bicrystal-instances", type=int, default=512)
     ap.add_argument("--no-bicrystal", action="store_true")
+    ap.add_argument("--candidates", type=int, default=65536)
+    ap.add_argument("--exhaustive", action="store_true", help="c5: also simulate every candidate")
     args = ap.parse_args()
     global GRID
     if args.grid:
@@ -582,6 +584,10 @@ def main():
         run_c3(args)
     elif args.workload == "accuracy":
         run_accuracy_study(args)
+    elif args.workload == "c5":
+        from mpf3d.screen import screen
+        rep = screen(n_candidates=args.candidates, exhaustive=args.exhaustive, seed=SEED)
+        print(json.dumps({"workload": "surrogate-screened orientation scan", **rep}), flush=True)
     else:
         run_ours(args, rank, world)
     if world > 1 and args.impl == "ours":
