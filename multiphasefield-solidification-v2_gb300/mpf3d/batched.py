@@ -221,7 +221,7 @@ class BatchedBicrystals:
             top = min(hl[i], hr[i]) - z_margin
             ks = np.arange(nz, dtype=np.float64)
             sel = (r[:, 1] > 0) & (ks >= z0) & (ks <= top)
-            if sel.sum() >= 3:
+            if sel.sum() >= 6:
                 xs = r[sel, 0] / r[sel, 1]
                 slope = np.polyfit(ks[sel], xs, 1)[0]
                 out[i] = math.degrees(math.atan(slope))
@@ -241,39 +241,46 @@ class BatchedBicrystals:
         return out.cpu().numpy()
 
     def run(self, steps: int, sample_every: int = 50, graph_steps: int = 50):
-        """Advance `steps` steps, sampling the fronts every `sample_every`
-        steps, and return per-instance velocities (cells/step fitted while
-        both fronts stay 6 cells below the top), their ratio and the final GB
-        inclination."""
+        """Advance `steps` steps, sampling the fronts and grain volumes every
+        `sample_every` steps.  Per instance, each grain's growth velocity
+        (cells/step) is the slope of its volume divided by its footprint
+        (its half of the base), fitted over the samples taken while both
+        fronts stay 6 cells below the top; returns the velocities, their ratio
+        (grain 1 / grain 2) and the final grain-boundary inclination."""
         if self.graph is None and graph_steps:
             self.capture(graph_steps)
-        times, h1, h2 = [0], [], []
-        a, b, _, _ = self.fronts()
-        h1.append(a)
-        h2.append(b)
+        times, h1, h2, V1, V2 = [0], [], [], [], []
+
+        def sample():
+            a, b, v1, v2 = self.fronts()
+            h1.append(a)
+            h2.append(b)
+            V1.append(v1)
+            V2.append(v2)
+
+        sample()
         done = 0
         while done < steps:
             k = min(sample_every, steps - done)
             self.step(k)
             done += k
-            a, b, _, _ = self.fronts()
             times.append(done)
-            h1.append(a)
-            h2.append(b)
+            sample()
         self.check()
         times = np.asarray(times, np.float64)
-        H1, H2 = np.stack(h1, 1), np.stack(h2, 1)
+        H1, H2, A1, A2 = (np.stack(x, 1) for x in (h1, h2, V1, V2))
         v1 = np.full(self.n, np.nan)
         v2 = np.full(self.n, np.nan)
         for i, (nx, ny, nz) in enumerate(self.dims):
             ok = (H1[i] < nz - 6) & (H2[i] < nz - 6)
             if ok.sum() >= 2:
-                v1[i] = np.polyfit(times[ok], H1[i, ok], 1)[0]
-                v2[i] = np.polyfit(times[ok], H2[i, ok], 1)[0]
+                split = nx // 2
+                v1[i] = np.polyfit(times[ok], A1[i, ok], 1)[0] / (split * ny)
+                v2[i] = np.polyfit(times[ok], A2[i, ok], 1)[0] / ((nx - split) * ny)
         with np.errstate(invalid="ignore", divide="ignore"):
             ratio = v1 / v2
         return {"v1": v1, "v2": v2, "velocity_ratio": ratio, "gb_angle_deg": self.gb_inclination(),
-                "times": times, "h1": H1, "h2": H2}
+                "times": times, "h1": H1, "h2": H2, "V1": A1, "V2": A2}
 
 
 def sample_batch(n: int, seed: int = 0, sizes_xy=(64, 96, 128), sizes_z=(64, 96), dT_range=(0.25, 3.0),

@@ -14,8 +14,16 @@ import time
 
 import numpy as np
 
-from .batched import BatchedBicrystals, sample_batch
+from .batched import BatchedBicrystals
 from .surrogate import Surrogate
+
+
+def bounded(y: np.ndarray) -> np.ndarray:
+    """Training form of the targets: the velocity ratio r mapped to
+    (r - 1)/(|r| + 1) -- (v1 - v2)/(v1 + v2) for growing grains, bounded and
+    monotone in r -- and the inclination in units of 45 degrees."""
+    y = np.asarray(y, np.float64)
+    return np.stack([(y[:, 0] - 1.0) / (np.abs(y[:, 0]) + 1.0), y[:, 1] / 45.0], 1)
 
 
 def sample_pairs(n: int, seed: int, dT_range=(0.25, 3.0), delta_a_range=(0.0, 1.0)):
@@ -25,7 +33,7 @@ def sample_pairs(n: int, seed: int, dT_range=(0.25, 3.0), delta_a_range=(0.0, 1.
     return q[:, 0], q[:, 1], rng.uniform(*dT_range, n), rng.uniform(*delta_a_range, n)
 
 
-def simulate(q1, q2, dT, da, dims=(32, 32, 48), steps=400, sample_every=10, batch=4096, base_height=16.0,
+def simulate(q1, q2, dT, da, dims=(32, 32, 64), steps=300, sample_every=10, batch=4096, base_height=16.0,
              device="cuda:0"):
     """Velocity ratio and grain-boundary inclination of every pair, simulated
     in batches of `batch` instances; returns ([n, 2] targets, GPU seconds)."""
@@ -48,11 +56,13 @@ def simulate(q1, q2, dT, da, dims=(32, 32, 48), steps=400, sample_every=10, batc
     return out, time.perf_counter() - t0
 
 
-def screen(n_candidates=65536, n_train=512, top_k=256, n_audit=256, seed=0, dims=(32, 32, 48), steps=400,
-           epochs=300, objective=1, exhaustive=False, device="cuda:0"):
+def screen(n_candidates=65536, n_train=512, top_k=256, n_audit=256, seed=0, dims=(32, 32, 64), steps=300,
+           epochs=300, objective=0, exhaustive=False, device="cuda:0"):
     """Rank n_candidates pairs by the surrogate's prediction of target
     `objective` (0 velocity ratio, 1 grain-boundary inclination; larger is
-    better) and check it by re-simulation.  Returns a report dict."""
+    better) and check it by re-simulation.  Errors and objective values are
+    reported in the bounded training form (see `bounded`).  Returns a report
+    dict."""
     import torch
 
     q1, q2, dT, da = sample_pairs(n_candidates, seed)
@@ -62,8 +72,8 @@ def screen(n_candidates=65536, n_train=512, top_k=256, n_audit=256, seed=0, dims
                                 device=device)
     t0 = time.perf_counter()
     s = Surrogate(seed=seed, device=device)
-    hist = s.fit(q1[train_idx], q2[train_idx], dT[train_idx], da[train_idx], y_train, epochs=epochs, batch=128,
-                 lr=2e-3)
+    hist = s.fit(q1[train_idx], q2[train_idx], dT[train_idx], da[train_idx], bounded(y_train), epochs=epochs,
+                 batch=128, lr=2e-3)
     torch.cuda.synchronize()
     t_fit = time.perf_counter() - t0
     t0 = time.perf_counter()
@@ -75,6 +85,7 @@ def screen(n_candidates=65536, n_train=512, top_k=256, n_audit=256, seed=0, dims
     audit = rng.choice(n_candidates, n_audit, replace=False)
     chk_idx = np.concatenate([top, audit])
     y_chk, t_chk = simulate(q1[chk_idx], q2[chk_idx], dT[chk_idx], da[chk_idx], dims, steps, device=device)
+    y_chk = bounded(y_chk)
     p_chk = pred[chk_idx]
 
     def err(a, b):
@@ -99,6 +110,7 @@ def screen(n_candidates=65536, n_train=512, top_k=256, n_audit=256, seed=0, dims
     report["gpu_seconds"]["screened_total"] = screened
     if exhaustive:
         y_all, t_all = simulate(q1, q2, dT, da, dims, steps, device=device)
+        y_all = bounded(y_all)
         truth = y_all[:, objective]
         fin = np.isfinite(truth)
         true_top = np.argsort(-np.where(fin, truth, -np.inf))[:top_k]
