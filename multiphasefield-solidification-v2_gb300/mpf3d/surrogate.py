@@ -21,16 +21,19 @@ import numpy as np
 
 from . import _lib
 
-IN_FEATURES = 10
-K1 = 16  # input features padded to the GEMM's k granularity
+IN_FEATURES = 10     # physical inputs: 2 quaternions, undercooling, anisotropy strength
+DERIVED = 4          # fixed facet-alignment features computed from the quaternions
+K1 = 16  # input columns of the first GEMM (k granularity of the tensor-core tile)
 HIDDEN = 256
 OUT = 2
 LAYERS = [(K1, HIDDEN, 1), (HIDDEN, HIDDEN, 1), (HIDDEN, HIDDEN, 1), (HIDDEN, OUT, 0)]  # (K, N, act)
 
 
-def n_params() -> int:
-    """Trainable parameters (the padded input columns excluded)."""
-    return IN_FEATURES * HIDDEN + HIDDEN + 2 * (HIDDEN * HIDDEN + HIDDEN) + HIDDEN * OUT + OUT
+def n_params(derived: bool = False) -> int:
+    """Trainable parameters of the 10 -> 256 -> 256 -> 256 -> 2 network (with
+    `derived`, also the first-layer weights of the 4 derived features)."""
+    k = IN_FEATURES + (DERIVED if derived else 0)
+    return k * HIDDEN + HIDDEN + 2 * (HIDDEN * HIDDEN + HIDDEN) + HIDDEN * OUT + OUT
 
 
 def canonical(q: np.ndarray) -> np.ndarray:
@@ -74,15 +77,34 @@ def qmul(a: np.ndarray, b: np.ndarray) -> np.ndarray:
                      aw * bw - ax * bx - ay * by - az * bz], -1)
 
 
+def facet_alignment(q: np.ndarray) -> np.ndarray:
+    """[M, 2]: the two largest |n . z| over a grain's rotated {111} normals --
+    how close its nearest facets lie to the growth direction z, which sets
+    a(theta) and b(theta) of a front normal to z.  Invariant under the cubic
+    group and under q -> -q."""
+    q = np.asarray(q, np.float64)
+    x, y, z, w = np.moveaxis(q / np.linalg.norm(q, axis=-1, keepdims=True), -1, 0)
+    # third row of the rotation matrix: z components of the rotated axes
+    r = np.stack([2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y)], -1)
+    base = np.array([[1, 1, 1], [1, 1, -1], [1, -1, 1], [-1, 1, 1]], np.float64) / np.sqrt(3.0)
+    c = np.sort(np.abs(r @ base.T), axis=-1)
+    return c[..., ::-1][..., :2]
+
+
 def features(q1, q2, undercooling, delta_a, dT_range=(0.25, 3.0)) -> np.ndarray:
-    """[M, 10] inputs: the two canonical quaternions, undercooling and
-    anisotropy strength mapped to [-1, 1]."""
+    """[M, 14] network input: the 10 physical inputs -- both canonical
+    quaternions, undercooling and anisotropy strength mapped to [-1, 1] --
+    followed by 4 fixed invariant features of the quaternions (the facet
+    alignment of each grain with z), which occupy 4 of the 6 padding columns
+    of the first GEMM."""
     q1 = canonical(q1)
     q2 = canonical(q2)
     lo, hi = dT_range
     dT = (np.asarray(undercooling, np.float64) - lo) / (hi - lo) * 2.0 - 1.0
     da = np.asarray(delta_a, np.float64) * 2.0 - 1.0
-    return np.concatenate([q1, q2, dT[:, None], da[:, None]], 1).astype(np.float32)
+    f1 = facet_alignment(q1) * 2.0 - 1.0
+    f2 = facet_alignment(q2) * 2.0 - 1.0
+    return np.concatenate([q1, q2, dT[:, None], da[:, None], f1, f2], 1).astype(np.float32)
 
 
 def augment(q1, q2, rng) -> tuple:
@@ -109,7 +131,7 @@ class Surrogate:
             bound = 1.0 / np.sqrt(fan_in)
             W = rng.uniform(-bound, bound, (N, K)).astype(np.float32)
             if K == K1:
-                W[:, IN_FEATURES:] = 0.0
+                W[:, IN_FEATURES + DERIVED:] = 0.0
             b = rng.uniform(-bound, bound, N).astype(np.float32)
             self.offsets.append((off, off + N * K))
             chunks += [W.ravel(), b]
@@ -148,11 +170,11 @@ class Surrogate:
         _lib.check(rc, "gemm_bf16")
 
     def prepare(self, X: np.ndarray):
-        """[M, 10] float features -> padded BF16 device input [M, 16]."""
+        """[M, <=16] float features -> zero-padded BF16 device input [M, 16]."""
         t = self.torch
         M = X.shape[0]
         xp = np.zeros((M, K1), np.float32)
-        xp[:, :IN_FEATURES] = X
+        xp[:, :X.shape[1]] = X
         x32 = t.from_numpy(xp).to(self.device)
         x16 = t.empty((M, K1), dtype=t.int16, device=self.device)
         self._bf16(x32, x16)
@@ -208,7 +230,7 @@ class Surrogate:
                 dY = dH
         # the padded input columns carry no parameters
         o, _ = self.offsets[0]
-        self.g.narrow(0, o, HIDDEN * K1).view(HIDDEN, K1)[:, IN_FEATURES:] = 0.0
+        self.g.narrow(0, o, HIDDEN * K1).view(HIDDEN, K1)[:, IN_FEATURES + DERIVED:] = 0.0
 
     def loss_and_grad(self, x16, target):
         """Weighted MSE on standardised targets; fills self.g, returns the loss."""

@@ -78,11 +78,11 @@ def cpu_forward_backward(layers, X, target, w):
 
 
 def test_backward_matches_cpu_float64_restatement():
-    from mpf3d.surrogate import Surrogate, LAYERS, IN_FEATURES, HIDDEN, K1
+    from mpf3d.surrogate import Surrogate, LAYERS, IN_FEATURES, DERIVED, HIDDEN, K1
     s = Surrogate(seed=3)
     rng = np.random.default_rng(0)
     M = 96
-    X = rng.uniform(-1, 1, (M, IN_FEATURES)).astype(np.float32)
+    X = rng.uniform(-1, 1, (M, IN_FEATURES + DERIVED)).astype(np.float32)
     T = rng.standard_normal((M, 2)).astype(np.float32)
     x16 = s.prepare(X)
     tT = torch.from_numpy(T).to("cuda:0")
@@ -90,7 +90,7 @@ def test_backward_matches_cpu_float64_restatement():
     g = s.g.cpu().numpy().astype(np.float64)
     layers = s.bf16_weights()
     Xp = np.zeros((M, K1))
-    Xp[:, :IN_FEATURES] = bf16_round(X)
+    Xp[:, :IN_FEATURES + DERIVED] = bf16_round(X)
     out, grads = cpu_forward_backward(layers, Xp, T.astype(np.float64), np.ones(2))
     gpu_out = s.forward(x16).cpu().numpy()
     assert np.abs(gpu_out - out).max() <= 2e-2 * max(1.0, np.abs(out).max())
@@ -101,7 +101,7 @@ def test_backward_matches_cpu_float64_restatement():
         rW, rb = grads[layer]
         if layer == 0:
             rW = rW.copy()
-            rW[:, IN_FEATURES:] = 0.0
+            rW[:, IN_FEATURES + DERIVED:] = 0.0
         for got, ref in ((gW, rW), (gb, rb)):
             err = np.linalg.norm(got - ref) / max(np.linalg.norm(ref), 1e-12)
             assert err <= 2e-2, f"layer {layer}: relative gradient error {err:.3e}"
