@@ -142,6 +142,29 @@ int mpf3d_compact_step(const uint32_t *head, const uint16_t *idx, const float *v
                        uint32_t *work_items, uint32_t *work_count, int parity, int32_t *err,
                        void *stream);
 
+/* Launch shape of the compact step (see mpf3d_compact_step_tuned).  Every
+ * shape computes the same result; only the scheduling differs. */
+typedef struct mpf3d_tuning {
+    int32_t sweep_zb;              /* cells per sweep thread along z: 2, 4 or 8 */
+    int32_t sweep_by;              /* sweep block = 32 x sweep_by threads: 4, 8 or 16 */
+    int32_t general_blocks_per_sm; /* general work-list kernel: blocks per SM, 1..64 */
+    int32_t general_threads;       /* and threads per block: 128 or 256 */
+    int32_t iface_blocks_per_sm;   /* interface work-list kernel: blocks per SM, 1..64 */
+    int32_t iface_threads;         /* and threads per block: 64 or 128 */
+} mpf3d_tuning;
+
+/* mpf3d_compact_step with an explicit launch shape (NULL: the default
+ * {4, 8, 8, 256, 8, 128}), as chosen by the package's autotuner.  No
+ * reference counterpart: the reference launches a fixed [4, 4, 4] block
+ * (config_3d.yaml gpu.threads_per_block). */
+int mpf3d_compact_step_tuned(const uint32_t *head, const uint16_t *idx, const float *val, uint32_t *head_out,
+                             uint16_t *idx_out, float *val_out, int slots, int amax, const double *T0z,
+                             double Tm_plus_cool, const float *wij, const float *a2ij, const float *mij,
+                             const float *n111, int N, int nx, int ny, int nz, const mpf3d_scalars *scalars,
+                             int enable_anisotropy, int enable_torque, int symmetric_normals,
+                             uint32_t *work_items, uint32_t *work_count, int parity, int32_t *err,
+                             void *stream, const mpf3d_tuning *tuning);
+
 /* compact state -> dense phi of one domain stored at cells [base, base +
  * nx*ny*nz) of state arrays whose slot planes are `stride` cells apart. */
 int mpf3d_compact_to_dense_view(const uint32_t *head, const uint16_t *idx, const float *val, int slots,

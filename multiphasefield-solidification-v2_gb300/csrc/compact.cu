@@ -558,9 +558,10 @@ __device__ __forceinline__ void push(const Queue &Q, int parity, bool want, bool
     }
 }
 
-constexpr int SWEEP_ZB = 4;  // cells per thread along z
+constexpr int SWEEP_ZB = 4;  // cells per thread along z (default; batches always use it)
 
-// The sweep of one column of SWEEP_ZB cells (l, m, k0..k0+ZB-1) of a domain.
+// The sweep of one column of ZB cells (l, m, k0..k0+ZB-1) of a domain.
+template <int ZB = SWEEP_ZB>
 __device__ __forceinline__ void sweep_column(const In &in, const Out &out, const Params &P, const Queue &Q, int parity,
                                              int l, int m, int k0) {
     const uint32_t plane = (uint32_t)P.nx * (uint32_t)P.ny;
@@ -570,14 +571,14 @@ __device__ __forceinline__ void sweep_column(const In &in, const Out &out, const
     const uint32_t dyp = (m < P.ny - 1) ? (uint32_t)P.nx : (uint32_t)(-(P.ny - 1) * P.nx);
     const uint32_t dym = (m > 0) ? (uint32_t)(-P.nx) : (uint32_t)((P.ny - 1) * P.nx);
     // heads of the column k0-1 .. k0+ZB (z clamped)
-    uint32_t hz[SWEEP_ZB + 2];
+    uint32_t hz[ZB + 2];
 #pragma unroll
-    for (int j = 0; j < SWEEP_ZB + 2; ++j) {
+    for (int j = 0; j < ZB + 2; ++j) {
         const int kk = min(max(k0 - 1 + j, 0), P.nz - 1);
         hz[j] = __ldg(in.head + (uint32_t)kk * plane + col);
     }
 #pragma unroll
-    for (int j = 0; j < SWEEP_ZB; ++j) {
+    for (int j = 0; j < ZB; ++j) {
         const int k = k0 + j;
         if (k >= P.nz) break;
         const uint32_t c = (uint32_t)k * plane + col;
@@ -611,17 +612,17 @@ __device__ __forceinline__ void sweep_column(const In &in, const Out &out, const
     }
 }
 
-template <int S, int AMAX>
-__global__ void __launch_bounds__(256) sweep_kernel(In in, Out out, Mats M, Params P, Queue Q, int parity,
+template <int S, int AMAX, int ZB = SWEEP_ZB>
+__global__ void __launch_bounds__(512) sweep_kernel(In in, Out out, Mats M, Params P, Queue Q, int parity,
                                                     int32_t *__restrict__ err) {
     const int l = blockIdx.x * blockDim.x + threadIdx.x;
     const int m = blockIdx.y * blockDim.y + threadIdx.y;
-    const int k0 = (blockIdx.z * blockDim.z + threadIdx.z) * SWEEP_ZB;
+    const int k0 = (blockIdx.z * blockDim.z + threadIdx.z) * ZB;
     if (blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.x < 2 && threadIdx.y == 0 &&
         threadIdx.z == 0)
         Q.count[2 * (parity ^ 1) + threadIdx.x] = 0;  // the previous step's kernels are done with them
     if (l >= P.nx || m >= P.ny || k0 >= P.nz) return;
-    sweep_column(in, out, P, Q, parity, l, m, k0);
+    sweep_column<ZB>(in, out, P, Q, parity, l, m, k0);
 }
 
 // Kernel 2 of a step: the cells queued for the general update, one thread
@@ -983,16 +984,34 @@ bool dims_ok(int nx, int ny, int nz) {
 
 template <int S, int AMAX>
 void launch_step(const In &in, const Out &out, const Mats &M, const Params &P, const Queue &Q, int parity,
-                 int32_t *err, cudaStream_t s) {
-    dim3 blk(32, 8, 1);
-    dim3 grd((P.nx + 31) / 32, (P.ny + 7) / 8, (P.nz + SWEEP_ZB - 1) / SWEEP_ZB);
-    sweep_kernel<S, AMAX><<<grd, blk, 0, s>>>(in, out, M, P, Q, parity, err);
+                 int32_t *err, cudaStream_t s, const mpf3d_tuning &T) {
+    const int by = T.sweep_by;
+    dim3 blk(32, by, 1);
+#define SWEEP_LAUNCH(ZB)                                                                                        \
+    sweep_kernel<S, AMAX, ZB><<<dim3((P.nx + 31) / 32, (P.ny + by - 1) / by, (P.nz + ZB - 1) / ZB), blk, 0, s>>>( \
+        in, out, M, P, Q, parity, err)
+    if (T.sweep_zb == 2) SWEEP_LAUNCH(2);
+    else if (T.sweep_zb == 8) SWEEP_LAUNCH(8);
+    else SWEEP_LAUNCH(4);
+#undef SWEEP_LAUNCH
     int dev = 0, sms = 148;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    general_kernel<S, AMAX><<<sms * 8, 256, 0, s>>>(in, out, M, P, Q, parity, err);
-    if (P.use_aniso) interface_kernel<S, AMAX><<<sms * 8, 128, 0, s>>>(in, out, M, P, Q, parity, err);
+    general_kernel<S, AMAX><<<sms * T.general_blocks_per_sm, T.general_threads, 0, s>>>(in, out, M, P, Q, parity, err);
+    if (P.use_aniso)
+        interface_kernel<S, AMAX><<<sms * T.iface_blocks_per_sm, T.iface_threads, 0, s>>>(in, out, M, P, Q, parity,
+                                                                                          err);
 }
+
+bool tuning_ok(const mpf3d_tuning &T) {
+    return (T.sweep_zb == 2 || T.sweep_zb == 4 || T.sweep_zb == 8) &&
+           (T.sweep_by == 4 || T.sweep_by == 8 || T.sweep_by == 16) && T.general_blocks_per_sm >= 1 &&
+           T.general_blocks_per_sm <= 64 && (T.general_threads == 128 || T.general_threads == 256) &&
+           T.iface_blocks_per_sm >= 1 && T.iface_blocks_per_sm <= 64 &&
+           (T.iface_threads == 64 || T.iface_threads == 128);
+}
+
+const mpf3d_tuning kDefaultTuning = {4, 8, 8, 256, 8, 128};
 
 }  // namespace
 
@@ -1052,13 +1071,15 @@ extern "C" int mpf3d_compact_active_count(const uint32_t *cnt, const uint16_t *i
     return cudaGetLastError() == cudaSuccess ? MPF3D_OK : MPF3D_ERR_CUDA;
 }
 
-extern "C" int mpf3d_compact_step(const uint32_t *cnt, const uint16_t *idx, const float *val, uint32_t *cnt_out,
-                                  uint16_t *idx_out, float *val_out, int slots, int amax, const double *T0z,
-                                  double Tm_plus_cool, const float *wij, const float *a2ij, const float *mij,
-                                  const float *n111, int N, int nx, int ny, int nz, const mpf3d_scalars *sc,
-                                  int enable_anisotropy, int enable_torque, int symmetric_normals,
-                                  uint32_t *work_items, uint32_t *work_count, int parity, int32_t *err,
-                                  void *stream) {
+extern "C" int mpf3d_compact_step_tuned(const uint32_t *cnt, const uint16_t *idx, const float *val,
+                                        uint32_t *cnt_out, uint16_t *idx_out, float *val_out, int slots, int amax,
+                                        const double *T0z, double Tm_plus_cool, const float *wij, const float *a2ij,
+                                        const float *mij, const float *n111, int N, int nx, int ny, int nz,
+                                        const mpf3d_scalars *sc, int enable_anisotropy, int enable_torque,
+                                        int symmetric_normals, uint32_t *work_items, uint32_t *work_count,
+                                        int parity, int32_t *err, void *stream, const mpf3d_tuning *tuning) {
+    const mpf3d_tuning T = tuning ? *tuning : kDefaultTuning;
+    if (!tuning_ok(T)) return MPF3D_ERR_ARG;
     if (!cnt || !idx || !val || !cnt_out || !idx_out || !val_out || !T0z || !wij || !a2ij || !mij || !n111 || !sc ||
         !err || !work_items || !work_count)
         return MPF3D_ERR_ARG;
@@ -1118,11 +1139,23 @@ extern "C" int mpf3d_compact_step(const uint32_t *cnt, const uint16_t *idx, cons
     Queue Q{work_items, work_count};
     parity &= 1;
     cudaStream_t s = (cudaStream_t)stream;
-    if (slots == 4 && amax == 8) launch_step<4, 8>(in, out, M, P, Q, parity, err, s);
-    else if (slots == 8 && amax == 16) launch_step<8, 16>(in, out, M, P, Q, parity, err, s);
-    else if (slots == 16 && amax == 32) launch_step<16, 32>(in, out, M, P, Q, parity, err, s);
+    if (slots == 4 && amax == 8) launch_step<4, 8>(in, out, M, P, Q, parity, err, s, T);
+    else if (slots == 8 && amax == 16) launch_step<8, 16>(in, out, M, P, Q, parity, err, s, T);
+    else if (slots == 16 && amax == 32) launch_step<16, 32>(in, out, M, P, Q, parity, err, s, T);
     else return MPF3D_ERR_ARG;
     return cudaGetLastError() == cudaSuccess ? MPF3D_OK : MPF3D_ERR_CUDA;
+}
+
+extern "C" int mpf3d_compact_step(const uint32_t *cnt, const uint16_t *idx, const float *val, uint32_t *cnt_out,
+                                  uint16_t *idx_out, float *val_out, int slots, int amax, const double *T0z,
+                                  double Tm_plus_cool, const float *wij, const float *a2ij, const float *mij,
+                                  const float *n111, int N, int nx, int ny, int nz, const mpf3d_scalars *sc,
+                                  int enable_anisotropy, int enable_torque, int symmetric_normals,
+                                  uint32_t *work_items, uint32_t *work_count, int parity, int32_t *err,
+                                  void *stream) {
+    return mpf3d_compact_step_tuned(cnt, idx, val, cnt_out, idx_out, val_out, slots, amax, T0z, Tm_plus_cool, wij,
+                                    a2ij, mij, n111, N, nx, ny, nz, sc, enable_anisotropy, enable_torque,
+                                    symmetric_normals, work_items, work_count, parity, err, stream, nullptr);
 }
 
 extern "C" int mpf3d_compact_to_dense_view(const uint32_t *head, const uint16_t *idx, const float *val, int slots,

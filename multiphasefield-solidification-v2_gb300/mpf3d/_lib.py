@@ -31,6 +31,13 @@ class Scalars(ctypes.Structure):
     _fields_ = [("v", ctypes.c_double * 13), ("f32mask", ctypes.c_uint32)]
 
 
+class Tuning(ctypes.Structure):
+    """mpf3d_tuning: launch shape of the compact step."""
+    _fields_ = [("sweep_zb", ctypes.c_int32), ("sweep_by", ctypes.c_int32),
+                ("general_blocks_per_sm", ctypes.c_int32), ("general_threads", ctypes.c_int32),
+                ("iface_blocks_per_sm", ctypes.c_int32), ("iface_threads", ctypes.c_int32)]
+
+
 # name -> (restype, argtypes)
 _SIGS = {
     "mpf3d_version": (_I32, []),
@@ -62,6 +69,9 @@ _SIGS = {
     "mpf3d_adam": (_I32, [_VP, _VP, _VP, _VP, _VP, _I64, ctypes.c_float, ctypes.c_float, ctypes.c_float,
                           ctypes.c_float, _I32, ctypes.c_float, _VP]),
     "mpf3d_f32_to_bf16": (_I32, [_VP, _VP, _I64, _VP]),
+    "mpf3d_compact_step_tuned": (_I32, [_VP, _VP, _VP, _VP, _VP, _VP, _I32, _I32, _VP, _F64, _VP, _VP, _VP, _VP,
+                                        _I32, _I32, _I32, _I32, ctypes.POINTER(Scalars), _I32, _I32, _I32,
+                                        _VP, _VP, _I32, _VP, _VP, ctypes.POINTER(Tuning)]),
     "mpf3d_compact_step_noalloc": (_I32, [_VP, _VP, _VP, _VP, _VP, _VP, _I32, _I32, _VP, _F64, _VP, _VP,
                                           _VP, _VP, _I32, _I32, _I32, _I32, ctypes.POINTER(Scalars),
                                           _I32, _I32, _I32, _VP, _VP]),

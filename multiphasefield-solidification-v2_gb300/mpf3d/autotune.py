@@ -1,0 +1,123 @@
+"""Autotuner for the compact step's launch shape.
+
+The reference launches every kernel with a fixed [4, 4, 4] block
+(config_3d.yaml gpu.threads_per_block).  Here the shape -- cells per sweep
+thread along z, sweep block height, and the grid and block sizes of the two
+work-list kernels -- is searched per problem (grid, phases, slots, model
+switches, GPU) by timing each candidate on the solver's own state with CUDA
+events, restoring the state before every trial.  All shapes compute identical
+results.  Winners are cached in a JSON file (MPF3D_TUNING_CACHE, default
+~/.cache/mpf3d/tuning.json).
+"""
+
+from __future__ import annotations
+
+import itertools
+import json
+import os
+
+from . import _lib
+
+DEFAULT = (4, 8, 8, 256, 8, 128)
+SWEEP = [(zb, by) for zb in (2, 4, 8) for by in (4, 8, 16)]
+QUEUE = [(g, gt, i, it) for (g, gt), (i, it) in itertools.product([(4, 256), (8, 256), (16, 128), (32, 128)],
+                                                                   [(4, 128), (8, 128), (16, 64), (32, 64)])]
+
+
+def cache_path() -> str:
+    return os.environ.get("MPF3D_TUNING_CACHE",
+                          os.path.join(os.path.expanduser("~"), ".cache", "mpf3d", "tuning.json"))
+
+
+def make(cfg) -> _lib.Tuning:
+    t = _lib.Tuning()
+    (t.sweep_zb, t.sweep_by, t.general_blocks_per_sm, t.general_threads, t.iface_blocks_per_sm,
+     t.iface_threads) = (int(v) for v in cfg)
+    return t
+
+
+def key_of(solver) -> str:
+    import torch
+
+    name = torch.cuda.get_device_name(solver.device)
+    return (f"{name}|{solver.nx}x{solver.ny}x{solver.nz}|N{solver.N}|S{solver.slots}|"
+            f"a{int(solver.anisotropy)}t{int(solver.torque)}")
+
+
+def _load() -> dict:
+    try:
+        with open(cache_path()) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+def _store(db: dict) -> None:
+    p = cache_path()
+    os.makedirs(os.path.dirname(p), exist_ok=True)
+    tmp = p + f".tmp{os.getpid()}"
+    with open(tmp, "w") as f:
+        json.dump(db, f, indent=1, sort_keys=True)
+    os.replace(tmp, p)
+
+
+def time_config(solver, cfg, steps: int) -> float:
+    """Milliseconds per step of `cfg` on the solver's current state (restored
+    afterwards)."""
+    import torch
+
+    snap = [t.clone() for t in solver.buf[solver.cur]]
+    cur, count = solver.cur, solver.step_count
+    prev = solver.tuning
+    solver.tuning = make(cfg)
+    stream = torch.cuda.current_stream(solver.device)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    try:
+        solver.launch_step(count + 1)  # warm-up of this shape
+        e0.record(stream)
+        for i in range(steps):
+            solver.launch_step(count + 2 + i)
+        e1.record(stream)
+        torch.cuda.synchronize(solver.device)
+        ms = e0.elapsed_time(e1) / steps
+    finally:
+        solver.tuning = prev
+        solver.cur, solver.step_count = cur, count
+        for dst, src in zip(solver.buf[cur], snap):
+            dst.copy_(src)
+        solver.work_count.zero_()
+    return ms
+
+
+def tune(solver, steps: int = 8, use_cache: bool = True) -> dict:
+    """Search the launch shape for `solver`; returns {"config", "ms_per_step",
+    "default_ms_per_step", "trials"} and sets solver.tuning."""
+    key = key_of(solver)
+    db = _load() if use_cache else {}
+    if use_cache and key in db:
+        solver.tuning = make(db[key]["config"])
+        return db[key]
+    trials = {}
+    base = time_config(solver, DEFAULT, steps)
+    trials[str(DEFAULT)] = base
+    best, best_ms = DEFAULT, base
+    # stage 1: the sweep shape with the default work-list shape
+    for zb, by in SWEEP:
+        cfg = (zb, by) + DEFAULT[2:]
+        if str(cfg) not in trials:
+            trials[str(cfg)] = time_config(solver, cfg, steps)
+        if trials[str(cfg)] < best_ms:
+            best, best_ms = cfg, trials[str(cfg)]
+    # stage 2: the work-list kernels with the best sweep shape
+    for q in QUEUE:
+        cfg = best[:2] + q
+        if str(cfg) not in trials:
+            trials[str(cfg)] = time_config(solver, cfg, steps)
+        if trials[str(cfg)] < best_ms:
+            best, best_ms = cfg, trials[str(cfg)]
+    solver.tuning = make(best)
+    rec = {"config": list(best), "ms_per_step": best_ms, "default_ms_per_step": base, "trials": trials}
+    if use_cache:
+        db[key] = rec
+        _store(db)
+    return rec

@@ -119,6 +119,7 @@ class CompactSolver:
         self.buf = [self._alloc(), self._alloc()]
         self.cur = 0
         self.step_count = 0
+        self.tuning = None  # launch shape (mpf3d_tuning); None = library default
         if owner_init is not None:
             owner, slab, prof = owner_init
             h, i_, v = self.buf[0]
@@ -171,14 +172,14 @@ class CompactSolver:
         src = self.buf[self.cur]
         dst = self.buf[1 - self.cur]
         tmc = self.T_melt + step_index * self.cooling_rate
-        rc = _lib.lib().mpf3d_compact_step(
+        rc = _lib.lib().mpf3d_compact_step_tuned(
             src[0].data_ptr(), src[1].data_ptr(), src[2].data_ptr(), dst[0].data_ptr(),
             dst[1].data_ptr(), dst[2].data_ptr(), self.slots, self.amax, self.T0z.data_ptr(), tmc,
             self.wij.data_ptr(), self.a2ij.data_ptr(), self.mij.data_ptr(), self.n111.data_ptr(),
             self.N, self.nx, self.ny, self.nz, ctypes.byref(self.scalars), int(self.anisotropy),
             int(self.torque), int(self.symmetric_normals), self.work_items.data_ptr(),
-            self.work_count.data_ptr(),
-            step_index & 1, self.err.data_ptr(), self._stream())
+            self.work_count.data_ptr(), step_index & 1, self.err.data_ptr(), self._stream(),
+            ctypes.byref(self.tuning) if self.tuning is not None else None)
         _lib.check(rc, "compact_step")
         self.cur = 1 - self.cur
 
@@ -221,6 +222,12 @@ class CompactSolver:
         i2[: old * self.cells].copy_(idx)
         v2[: old * self.cells].copy_(val)
         self.step_count = steps
+
+    def autotune(self, steps: int = 8, use_cache: bool = True) -> dict:
+        """Pick the fastest launch shape for this problem (see mpf3d.autotune)."""
+        from . import autotune
+
+        return autotune.tune(self, steps=steps, use_cache=use_cache)
 
     def check(self) -> None:
         v = int(self.err.item())

@@ -111,3 +111,27 @@ def test_owner_map_start_equals_dense_start():
     a.step(3)
     b.step(3)
     assert np.array_equal(a.to_dense(), b.to_dense())
+
+
+def test_every_launch_shape_gives_the_same_state(tmp_path, monkeypatch):
+    """The autotuner's candidates only reschedule the work: results are bit
+    identical; the tuner restores the state it timed on and caches its pick."""
+    from mpf3d import autotune, inputs
+    monkeypatch.setenv("MPF3D_TUNING_CACHE", str(tmp_path / "tuning.json"))
+    case = inputs.voronoi_case(40, 24, 36, 7, 10, seed=12, orientation_seed=1)
+    ref = make_solver(case)
+    ref.step(4)
+    want = ref.to_dense()
+    for cfg in [(2, 4, 4, 256, 4, 128), (8, 16, 32, 128, 32, 64), (4, 8, 16, 128, 16, 64)]:
+        s = make_solver(case)
+        s.tuning = autotune.make(cfg)
+        s.step(4)
+        assert np.array_equal(s.to_dense(), want), cfg
+    s = make_solver(case)
+    before = s.to_dense()
+    rec = s.autotune(steps=2)
+    assert np.array_equal(s.to_dense(), before)
+    assert len(rec["config"]) == 6 and rec["ms_per_step"] <= rec["default_ms_per_step"]
+    s.step(4)
+    assert np.array_equal(s.to_dense(), want)
+    assert (tmp_path / "tuning.json").exists()
