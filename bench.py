@@ -239,10 +239,14 @@ def run_ours(args, rank, world):
         if world > 1:
             torch.distributed.barrier()
 
-    # warm-up, then restart the job from the initial state
+    # warm-up (including the launch-shape search), then restart the job from
+    # the initial state with the chosen shape
     solver.step(args.warmup)
+    tuned = solver.autotune(steps=8) if not args.no_autotune else None
     torch.cuda.synchronize(dev)
+    tuning = solver.tuning
     solver = CompactSolver(phi0, temp, n111, wij, aij, mij, phys, slots=args.slots)
+    solver.tuning = tuning
     torch.cuda.synchronize(dev)
 
     e0 = torch.cuda.Event(enable_timing=True)
@@ -267,6 +271,7 @@ def run_ours(args, rank, world):
     # accounting pass (untimed): record bytes of the state before and after
     # every step, and the stored-phase occupancy
     acc = CompactSolver(phi0, temp, n111, wij, aij, mij, phys, slots=args.slots)
+    acc.tuning = tuning
     occ = [int(acc.stored_counts().sum(dtype=torch.int64).item())]
     rec = [acc.record_bytes()]
     for i in range(args.steps):
@@ -290,7 +295,8 @@ def run_ours(args, rank, world):
     if args.no_e2e:
         t_e2e, in_bytes, out_bytes = float("nan"), 0, 0
     else:
-        t_e2e, in_bytes, out_bytes = e2e_run(args, phi0, temp, n111, wij, aij, mij, phys, dev, barrier, world)
+        t_e2e, in_bytes, out_bytes = e2e_run(args, phi0, temp, n111, wij, aij, mij, phys, dev, barrier, world,
+                                             tuning)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -298,7 +304,8 @@ def run_ours(args, rank, world):
         cpu = {"value": v, "unit": UNIT, "cores": th, "kind": "port",
                "sample": f"64x64x256 crop of the workload (N=65), {st} oracle steps (reference "
                          f"float32 typing), OpenMP"}
-    extra = {}
+    extra = {"launch_shape": {"config": list(tuned["config"]), "ms_per_step_tuned": tuned["ms_per_step"],
+                              "ms_per_step_default": tuned["default_ms_per_step"]} if tuned else None}
     if rank == 0 and not args.no_accuracy and args.accuracy_steps > 0:
         del solver
         torch.cuda.empty_cache()
@@ -311,7 +318,7 @@ def run_ours(args, rank, world):
          traffic, bytes_per_launch, occ, clk, cpu, final_cnt_sum, extra)
 
 
-def e2e_run(args, phi0, temp, n111, wij, aij, mij, phys, dev, barrier, world):
+def e2e_run(args, phi0, temp, n111, wij, aij, mij, phys, dev, barrier, world, tuning=None):
     import torch
     from mpf3d.solver import CompactSolver
     phi_host = phi0.cpu().pin_memory()
@@ -321,6 +328,7 @@ def e2e_run(args, phi0, temp, n111, wij, aij, mij, phys, dev, barrier, world):
     t0 = time.perf_counter()
     dphi = phi_host.to(dev, non_blocking=True)
     s2 = CompactSolver(dphi, temp, n111, wij, aij, mij, phys, slots=args.slots)
+    s2.tuning = tuning
     s2.step(args.steps, check=False)
     out_host.copy_(s2.to_dense(host=False), non_blocking=True)
     torch.cuda.synchronize(dev)
@@ -472,7 +480,8 @@ def emit(args, rank, world, value, ms, cells, t_e2e, in_bytes, out_bytes, achiev
                              "frac": achieved / peak, "traffic": traffic,
                              "peak_source": peak_kind,
                              "bytes_per_cell_step": bytes_per_launch / cells,
-                             "kernel": f"sweep+general+interface kernels <{args.slots},{2 * args.slots}>"},
+                             "kernel": f"sweep+general+interface kernels <{args.slots},{2 * args.slots}>",
+                             "traffic_unit": "bytes per step (3 launches), from the committed ncu summary"},
                 "stored_phases_per_cell": {"start": occ[0] / cells, "end": occ[-1] / cells},
                 "clocks": clk.summary(),
                 "cpu_baseline": cpu}
@@ -558,6 +567,7 @@ def main():
     ap.add_argument("--slots", type=int, default=16)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end run (profiling)")
+    ap.add_argument("--no-autotune", action="store_true", help="use the default launch shape")
     ap.add_argument("--grid", type=int, nargs=3, default=None,
                     help="override the 256^3 grid (smaller cases for profiling)")
     ap.add_argument("--accuracy-steps", type=int, default=100)
