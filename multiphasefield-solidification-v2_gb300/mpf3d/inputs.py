@@ -204,3 +204,43 @@ def voronoi_case(nx, ny, nz, n_grains, slab, seed=0, orientation_seed=1, phys: P
     q = random_quaternions(n_grains, orientation_seed)
     wij, aij, mij = matrices_for(phys, n_grains + 1)
     return Case(phi, temp, q, rotated_n111(q), wij, aij, mij, phys)
+
+
+def grain_map_2d(nx: int, ny: int, n_solid: int, seed: int) -> np.ndarray:
+    """[nx, ny] int32 grain ids 1..n_solid: nearest of n_solid seed points
+    drawn uniformly in the x-y plane from default_rng(seed) (x coordinates
+    first, then y); the columnar map of generate_random_grain_map_3d,
+    src/seed_modes_3d.py:15-24."""
+    rng = np.random.default_rng(seed)
+    sx = rng.uniform(0, nx, n_solid).reshape(-1, 1, 1)
+    sy = rng.uniform(0, ny, n_solid).reshape(-1, 1, 1)
+    lx = np.arange(nx, dtype=np.float32).reshape(1, nx, 1)
+    ly = np.arange(ny, dtype=np.float32).reshape(1, 1, ny)
+    return (np.argmin((lx - sx) ** 2 + (ly - sy) ** 2, axis=0) + 1).astype(np.int32)
+
+
+def phi_from_grain_map_2d(gmap: np.ndarray, n_solid: int, nz: int, dz: float, delta: float, height: float):
+    """Columnar phi [n_solid+1, nx, ny, nz]: each column's grain holds the tanh
+    profile of the front at `height` (init_phi_from_grain_map_3d,
+    src/seed_modes_3d.py:38-57)."""
+    nx, ny = gmap.shape
+    prof = tanh_profile(nz, height, dz, delta)
+    phi = np.zeros((n_solid + 1, nx, ny, nz), np.float32)
+    for g in range(1, n_solid + 1):
+        phi[g] = np.where((gmap == g)[:, :, None], prof[None, None, :], 0.0)
+    phi[0] = np.clip(1.0 - phi[1:].sum(axis=0), 0.0, 1.0)
+    return phi
+
+
+def wavy_front(nx: int, ny: int, nz: int, dz: float, delta: float, base: float, amplitude: float,
+               phase: float = 0.0) -> np.ndarray:
+    """Single grain under a front at base + amplitude*cos(2 pi x/nx + phase)
+    (amplitude 0: flat), liquid = 1 - solid; [2, nx, ny, nz] float32."""
+    x = np.arange(nx, dtype=np.float64).reshape(nx, 1, 1)
+    z = np.arange(nz, dtype=np.float64).reshape(1, 1, nz)
+    height = base + amplitude * np.cos(2.0 * math.pi * x / max(nx, 1) + phase)
+    solid = (0.5 * (1.0 - np.tanh(np.float32(2.2 / delta) * ((z - height) * dz)))).astype(np.float32)
+    phi = np.zeros((2, nx, ny, nz), np.float32)
+    phi[1] = np.broadcast_to(solid, (nx, ny, nz))
+    phi[0] = 1.0 - phi[1]
+    return phi
