@@ -84,6 +84,27 @@ int mpf3d_dense_update(const void *phi, void *phi_new, int phi_dtype, const void
 int mpf3d_dense_temp(void *temp, int temp_dtype, double cooling_rate, int rate_is_f32, int64_t n,
                      void *stream);
 
+/* ---- dense 2D kernels (reference numerics) --------------------------------
+ * The reference's 2D module src/gpu_kernels.py, on its dense [N][nx][ny]
+ * arrays (x periodic, y mirror).  The reference's verification suite runs it
+ * beside the 3D step (tests/verification_3d.py:21-25, 1509-1535). */
+
+/* Replaces kernel_update_nfmf, src/gpu_kernels.py:337-358.  Writes past
+ * `depth` rows are dropped and set MPF3D_DEV_MF_DEPTH. */
+int mpf2d_dense_apt(const void *phi, int phi_dtype, int N, int nx, int ny, int32_t *mf, int depth,
+                    int32_t *nf, int32_t *err, void *stream);
+
+/* Replaces kernel_update_phasefield_active, src/gpu_kernels.py:361-517.
+ * N >= 2: the reference's dominant-solid lookup defaults to grain 1. */
+int mpf2d_dense_update(const void *phi, void *phi_new, int phi_dtype, const void *temp, int temp_dtype,
+                       const int32_t *mf, int depth, const int32_t *nf, const float *wij,
+                       const float *aij, const float *mij, const float *n111, int N, int nx, int ny,
+                       const mpf3d_scalars *scalars, int32_t *err, void *stream);
+
+/* Replaces kernel_update_temp, src/gpu_kernels.py:520-525. */
+int mpf2d_dense_temp(void *temp, int temp_dtype, double cooling_rate, int rate_is_f32, int nx, int ny,
+                     void *stream);
+
 /* ---- compact FP32 tier (fused step) -------------------------------------
  * State of one buffer (x fastest: cell = (k*ny + m)*nx + l):
  *   head uint32[cells]        bits 0-6 number n of stored phases (phi > 0),

@@ -24,6 +24,7 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I" + INCLUD
 # (source, extra flags).  The reference-numerics tier forbids FMA contraction.
 SOURCES = [
     ("dense_ref.cu", ["-fmad=false"]),
+    ("dense2d.cu", ["-fmad=false"]),
     ("compact.cu", []),
     ("mlp.cu", []),
 ]

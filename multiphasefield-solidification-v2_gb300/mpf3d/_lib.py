@@ -46,6 +46,10 @@ _SIGS = {
                                   _I32, _I32, _I32, _I32, ctypes.POINTER(Scalars), _I32, _I32, _I32,
                                   _VP, _VP]),
     "mpf3d_dense_temp": (_I32, [_VP, _I32, _F64, _I32, _I64, _VP]),
+    "mpf2d_dense_apt": (_I32, [_VP, _I32, _I32, _I32, _I32, _VP, _I32, _VP, _VP, _VP]),
+    "mpf2d_dense_update": (_I32, [_VP, _VP, _I32, _VP, _I32, _VP, _I32, _VP, _VP, _VP, _VP, _VP,
+                                  _I32, _I32, _I32, ctypes.POINTER(Scalars), _VP, _VP]),
+    "mpf2d_dense_temp": (_I32, [_VP, _I32, _F64, _I32, _I32, _I32, _VP]),
     "mpf3d_compact_from_dense": (_I32, [_VP, _I32, _I32, _I32, _I32, _I32, _I32, _VP, _VP, _VP, _VP, _VP]),
     "mpf3d_compact_to_dense": (_I32, [_VP, _VP, _VP, _I32, _I32, _I32, _I32, _I32, _VP, _I32, _VP]),
     "mpf3d_compact_active_count": (_I32, [_VP, _VP, _I32, _I32, _I32, _I32, _VP, _VP]),

@@ -1,4 +1,5 @@
-"""CPU oracle for the 3D multi-phase-field step (ctypes front of mpf3d_oracle.c).
+"""CPU oracle for the 3D multi-phase-field step (ctypes front of mpf3d_oracle.c)
+and for the reference's 2D kernels (mpf2d_oracle.c).
 
 TEST INFRASTRUCTURE ONLY: imported by ``tests/``, ``__graft_entry__.smoke()``
 and the CPU-baseline leg of ``bench.py`` as the checker.  The product path
@@ -20,6 +21,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 SRC = os.path.join(HERE, "mpf3d_oracle.c")
+SRC2D = os.path.join(HERE, "mpf2d_oracle.c")
 BUILD_DIR = os.path.join(HERE, "_build")
 LIB_PATH = os.path.join(BUILD_DIR, "libmpf3d_oracle.so")
 
@@ -35,10 +37,12 @@ class Scalars(ctypes.Structure):
 def build(force: bool = False) -> str:
     """Compile the oracle with gcc (OpenMP, no FP contraction)."""
     os.makedirs(BUILD_DIR, exist_ok=True)
-    if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < os.path.getmtime(SRC):
+    stale = not os.path.exists(LIB_PATH) or any(os.path.getmtime(LIB_PATH) < os.path.getmtime(f)
+                                                for f in (SRC, SRC2D))
+    if force or stale:
         tmp = LIB_PATH + f".tmp{os.getpid()}"
         subprocess.check_call(["gcc", "-O2", "-std=c11", "-fopenmp", "-ffp-contract=off", "-fPIC",
-                               "-shared", "-o", tmp, SRC, "-lm"])
+                               "-shared", "-o", tmp, SRC, SRC2D, "-lm"])
         os.replace(tmp, LIB_PATH)
     return LIB_PATH
 
@@ -59,6 +63,11 @@ def lib():
         L.mpf3d_oracle_update.argtypes = ([vp, vp, i32, vp, i32, vp, i32, vp, vp, vp, vp, vp]
                                           + [i32] * 4 + [ctypes.POINTER(Scalars)] + [i32] * 4)
         L.mpf3d_oracle_update.restype = i32
+        L.mpf2d_oracle_apt.argtypes = [vp, i32, i32, i32, i32, vp, i32, vp]
+        L.mpf2d_oracle_apt.restype = i32
+        L.mpf2d_oracle_update.argtypes = ([vp, vp, i32, vp, i32, vp, vp, vp, vp, vp, vp] + [i32] * 3
+                                          + [ctypes.POINTER(Scalars), i32])
+        L.mpf2d_oracle_update.restype = i32
         _LIB = L
     return _LIB
 
@@ -133,3 +142,45 @@ def run(phi0, temp0, wij, aij, mij, n111, scalars: Scalars, steps, *, cooling_ra
         if record:
             hist.append((phi.copy(), nf.copy(), mf.copy(), st.copy(), temp.copy()))
     return (phi, temp, nf, mf, hist) if record else (phi, temp, nf, mf)
+
+
+# --- 2D kernels (src/gpu_kernels.py) -------------------------------------
+
+def apt2d(phi: np.ndarray, mf: np.ndarray, nf: np.ndarray) -> int:
+    """kernel_update_nfmf (src/gpu_kernels.py:337-358); -1 if mf is too shallow."""
+    N, nx, ny = phi.shape
+    return lib().mpf2d_oracle_apt(_ptr(phi), int(phi.dtype == np.float64), N, nx, ny, _ptr(mf), mf.shape[0],
+                                  _ptr(nf))
+
+
+def update2d(phi, phi_new, temp, mf, nf, wij, aij, mij, n111, scalars: Scalars, kmax=KMAX) -> int:
+    """kernel_update_phasefield_active (src/gpu_kernels.py:361-517)."""
+    N, nx, ny = phi.shape
+    assert phi_new.dtype == phi.dtype
+    for a in (wij, aij, mij, n111):
+        assert a.dtype == np.float32
+    return lib().mpf2d_oracle_update(
+        _ptr(phi), _ptr(phi_new), int(phi.dtype == np.float64), _ptr(temp), int(temp.dtype == np.float64),
+        _ptr(mf), _ptr(nf), _ptr(wij), _ptr(aij), _ptr(mij), _ptr(n111), N, nx, ny, ctypes.byref(scalars), kmax)
+
+
+def run2d(phi0, temp0, wij, aij, mij, n111, scalars: Scalars, steps, *, cooling_rate=0.0, rate_f32=True,
+          cooling=True, depth=None, kmax=KMAX):
+    """Run `steps` 2D reference steps (temperature, APT, update, swap), in the
+    order of the reference's run_2d_simulation (tests/verification_3d.py:939-1000)."""
+    phi = np.ascontiguousarray(phi0).copy()
+    phi_new = phi.copy()
+    temp = np.ascontiguousarray(temp0).copy()
+    N, nx, ny = phi.shape
+    mf = np.zeros((depth or max(N, 18), nx, ny), np.int32)
+    nf = np.zeros((nx, ny), np.int32)
+    for _ in range(steps):
+        if cooling and cooling_rate != 0.0:
+            temp_step(temp, cooling_rate, rate_f32)
+        if apt2d(phi, mf, nf) != 0:
+            raise RuntimeError("oracle 2D APT: mf too shallow")
+        rc = update2d(phi, phi_new, temp, mf, nf, wij, aij, mij, n111, scalars, kmax)
+        if rc != 0:
+            raise RuntimeError(f"oracle 2D update failed rc={rc}")
+        phi, phi_new = phi_new, phi
+    return phi, temp, nf, mf

@@ -9,11 +9,16 @@ GOLDEN = os.path.join(HERE, "golden")
 
 
 def golden_files(kind="run"):
+    """Golden fixtures of one kind: "run" (3D step sequences), "run2d" (2D
+    step sequences) or "apt" (APT known answers)."""
     out = []
     for f in sorted(glob.glob(os.path.join(GOLDEN, "*.npz"))):
         g = np.load(f)
-        is_run = "phi" in g.files
-        if (kind == "run") == is_run:
+        if "phi" not in g.files:
+            k = "apt"
+        else:
+            k = "run2d" if g["phi0"].ndim == 3 else "run"
+        if k == kind:
             out.append(f)
     return out
 
@@ -25,7 +30,7 @@ def golden_id(f):
 def valid_mf_equal(mf_a, mf_b, nf):
     """mf entries below nf agree (rows at or above nf are stale by design)."""
     d = min(mf_a.shape[0], mf_b.shape[0])
-    depth = np.arange(d)[:, None, None, None]
+    depth = np.arange(d).reshape((d,) + (1,) * nf.ndim)
     mask = depth < nf[None]
     if int(nf.max()) > d:
         return False

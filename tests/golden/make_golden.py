@@ -1,6 +1,7 @@
 """Generate the golden vectors under ``tests/golden`` by running the reference's
-own 3D kernel source (``src/gpu_kernels_3d.py``) on the CPU through
-``numba_typing_shim`` (compiled-Numba typing, serial grid loop).
+own kernel sources (the 3D ``src/gpu_kernels_3d.py`` and the 2D
+``src/gpu_kernels.py``) on the CPU through ``numba_typing_shim``
+(compiled-Numba typing, serial grid loop).
 
 Test infrastructure only.  Usage (needs a checkout of the reference)::
 
@@ -10,8 +11,9 @@ Inputs are built with the reference's own host helpers
 (``src/seed_modes_3d.py``, ``src/orientation_utils.py``, ``src/seed_modes.py``)
 imported from that checkout; the step sequence follows the reference's
 drivers: ``tests/verification_3d.py:830-893`` (temperature, checked APT,
-switchable update, swap) and ``run_randommode_3d.py:267-287`` (temperature,
-APT, update, swap).  Each case is written to ``<name>.npz``.
+switchable update, swap), ``run_randommode_3d.py:267-287`` (temperature,
+APT, update, swap) and, for the 2D kernels, ``tests/verification_3d.py:939-1000``
+(run_2d_simulation).  Each case is written to ``<name>.npz``.
 """
 
 from __future__ import annotations
@@ -126,6 +128,76 @@ def run_case(ref, name, phi0, temp0, quats, p, *, steps, f64, kernel="switchable
           f"({time.time() - t0:.1f}s)")
 
 
+def run_case_2d(ref, name, phi0, temp0, quats, p, *, steps, f64, out_dir=HERE):
+    """Steps of the reference's 2D kernels in run_2d_simulation's order
+    (tests/verification_3d.py:970-1000): temperature when the cooling rate is
+    non-zero, APT, update, swap."""
+    om = ref["orientation_utils"]
+    sm = ref["seed_modes"]
+    K = ref["kernels2d"]
+    d = derived(p)
+    N, nx, ny = phi0.shape
+    n111 = om.compute_rotated_n111(quats).astype(np.float32)
+    wij, aij, mij = sm.build_interaction_matrices(N, d["eps0_sl"], d["w0_sl"], d["m_sl_phi"],
+                                                  d["eps_gb"], d["w_gb"], d["m_gb_phi"])
+    wij, aij, mij = (a.astype(np.float32) for a in (wij, aij, mij))
+    phi_dt = np.float64 if f64 else np.float32
+    phi = phi0.astype(phi_dt).copy()
+    phi_new = phi.copy()
+    temp = temp0.copy()
+    depth = max(20, N, 18)
+    mf = np.zeros((depth, nx, ny), np.int32)
+    nf = np.zeros((nx, ny), np.int32)
+    sc = scalars_of(p, d)
+    scal32 = not f64
+    sargs = [shim.scalar(sc[k], scal32) for k in SCALAR_NAMES]
+    rate = shim.scalar(d["cooling_rate"], scal32)
+    threads = (4, 4)
+    blocks = tuple(math.ceil(n / 4) for n in (nx, ny))
+    T = shim.TypedArray
+    out = dict(phi0=phi0.astype(phi_dt), temp0=temp0.copy(), wij=wij, aij=aij, mij=mij, n111=n111,
+               quats=quats, scalars=np.array([sc[k] for k in SCALAR_NAMES]),
+               scalar_names=np.array(SCALAR_NAMES), scalars_f32=np.int32(scal32),
+               cooling_rate=np.float64(d["cooling_rate"]), steps=np.int32(steps))
+    phis, nfs, mfs, temps = [], [], [], []
+    t0 = time.time()
+    for _ in range(steps):
+        if d["cooling_rate"] != 0.0:
+            K.kernel_update_temp[blocks, threads](T(temp), rate, nx, ny)
+        K.kernel_update_nfmf[blocks, threads](T(phi), T(mf), T(nf), nx, ny, N)
+        K.kernel_update_phasefield_active[blocks, threads](
+            T(phi), T(phi_new), T(temp), T(mf), T(nf), T(wij, read_as_f64=True), T(aij), T(mij), T(n111),
+            nx, ny, N, *sargs)
+        phi, phi_new = phi_new, phi
+        phis.append(phi.copy())
+        nfs.append(nf.copy())
+        mfs.append(mf[: max(1, int(nf.max()))].copy())
+        temps.append(temp.copy())
+    out.update(phi=np.stack(phis), nf=np.stack(nfs), temp=np.stack(temps))
+    dmax = max(m.shape[0] for m in mfs)
+    mf_all = np.full((steps, dmax, nx, ny), -1, np.int32)
+    for s_, m in enumerate(mfs):
+        mf_all[s_, : m.shape[0]] = m
+    out["mf"] = mf_all
+    np.savez_compressed(os.path.join(out_dir, f"{name}.npz"), **out)
+    print(f"{name}: grid {nx}x{ny} N={N} steps={steps} f64={f64} nf_max={int(nf.max())} "
+          f"({time.time() - t0:.1f}s)")
+
+
+def stripes_phi_2d(nx, ny, n_solid, dx, delta, base, amp):
+    """Solid stripes along x under a cosine front, liquid above (float32)."""
+    x = np.arange(nx, dtype=np.float64).reshape(nx, 1)
+    y = np.arange(ny, dtype=np.float64).reshape(1, ny)
+    height = base + amp * np.cos(2.0 * math.pi * x / nx + 0.3)
+    solid = (0.5 * (1.0 - np.tanh(np.float32(2.2 / delta) * (y - height) * dx))).astype(np.float32)
+    phi = np.zeros((n_solid + 1, nx, ny), np.float32)
+    edges = np.linspace(0, nx, n_solid + 1).astype(int)
+    for g in range(1, n_solid + 1):
+        phi[g, edges[g - 1]:edges[g], :] = solid[edges[g - 1]:edges[g], :]
+    phi[0] = 1.0 - phi[1:].sum(axis=0)
+    return phi
+
+
 def apt_case(ref, name, phi, out_dir=HERE):
     K = ref["kernels"]
     N, nx, ny, nz = phi.shape
@@ -150,6 +222,8 @@ def main():
     import importlib
 
     ref = dict(kernels=shim.load_reference_kernels(os.path.join(args.reference, "src", "gpu_kernels_3d.py")),
+               kernels2d=shim.load_reference_kernels(os.path.join(args.reference, "src", "gpu_kernels.py"),
+                                                     "reference_gpu_kernels_2d"),
                orientation_utils=importlib.import_module("src.orientation_utils"),
                seed_modes=importlib.import_module("src.seed_modes"),
                seed_modes_3d=importlib.import_module("src.seed_modes_3d"))
@@ -216,6 +290,32 @@ def main():
         run_case(ref, "junction_f64", phij, tj, qj, p, steps=3, f64=True)
     if want("junction_f32"):
         run_case(ref, "junction_f32", phij, tj.astype(np.float32), qj, p, steps=3, f64=False)
+
+    # 2D kernels.  two_d_limit_2d is the 2D half of two_d_limit_consistency
+    # (tests/verification_3d.py:1509-1535): 12x14, one grain under a cosine
+    # front at 4.8 +- 1.2 cells, delta_a = 0, ksi = 1, T_melt - 4, 6 steps.
+    vparams = dict(p, delta_a=0.0, ksi=1.0)
+    vd = derived(vparams)
+    x = np.arange(12, dtype=np.float64).reshape(12, 1)
+    y = np.arange(14, dtype=np.float64).reshape(1, 14)
+    h2 = 4.8 + 1.2 * np.cos(2.0 * math.pi * x / 12)
+    s2 = (0.5 * (1.0 - np.tanh(np.float32(2.2 / vd["delta"]) * (y - h2) * p["dx"]))).astype(np.float32)
+    phi2 = np.zeros((2, 12, 14), np.float32)
+    phi2[1] = s2
+    phi2[0] = 1.0 - phi2[1]
+    qid = np.array([[0.0, 0.0, 0.0, 1.0], [0.0, 0.0, 0.0, 1.0]])
+    if want("two_d_limit_2d"):
+        run_case_2d(ref, "two_d_limit_2d", phi2, np.full((12, 14), np.float32(p["T_melt"] - 4.0), np.float32),
+                    qid, vparams, steps=6, f64=False)
+    # Anisotropic multi-grain 2D fronts: three stripes meeting a wavy front.
+    phis = stripes_phi_2d(15, 12, 3, p["dx"], d["delta"], 5.0, 1.5)
+    q3 = om.assign_quaternions_to_grains(3, mode="random", orientation_seed=31)
+    t2 = np.full((15, 12), np.float32(p["T_melt"] - 3.0), np.float32)
+    if want("stripes2d_f32"):
+        run_case_2d(ref, "stripes2d_f32", phis, t2, q3, p, steps=3, f64=False)
+    if want("stripes2d_f64"):
+        run_case_2d(ref, "stripes2d_f64", phis, t2.astype(np.float64), q3, dict(p, p_round=0.02), steps=3,
+                    f64=True)
 
     # APT known answers: boundary probes and the crafted KMAX overflow
     # (tests/verification_3d.py:1459-1480, 1538-1565).

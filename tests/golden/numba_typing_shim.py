@@ -1,5 +1,5 @@
 """Typing-faithful CPU stand-in for the parts of ``numba.cuda`` that the
-reference's 3D kernels use, so that the reference's own kernel source can be
+reference's 3D and 2D kernels use, so that the reference's own kernel source can be
 executed on the host to produce golden vectors.
 
 Test infrastructure only: nothing in the product imports this module.
@@ -217,7 +217,7 @@ class _Atomic:
 class _Local:
     @staticmethod
     def array(n, dtype):
-        assert dtype is float32, "only float32 local arrays are used by the 3D kernels"
+        assert dtype is float32, "only float32 local arrays are used by the reference kernels"
         return _LocalF32Array(n)
 
 
@@ -269,10 +269,10 @@ def install() -> None:
     sys.modules["numba.cuda"] = _CUDA
 
 
-def load_reference_kernels(path: str):
-    """Execute the reference's kernel module under the shim and return it."""
+def load_reference_kernels(path: str, name: str = "reference_gpu_kernels_3d"):
+    """Execute a reference kernel module (3D or 2D) under the shim and return it."""
     install()
-    spec = importlib.util.spec_from_file_location("reference_gpu_kernels_3d", path)
+    spec = importlib.util.spec_from_file_location(name, path)
     mod = importlib.util.module_from_spec(spec)
     spec.loader.exec_module(mod)
     mod.math = _MathShim

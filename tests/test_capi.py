@@ -17,7 +17,7 @@ def declared_functions():
     for f in os.listdir(os.path.join(ROOT, "include")):
         if f.endswith(".h"):
             txt = open(os.path.join(ROOT, "include", f)).read()
-            names += re.findall(r"^\s*(?:int|void|int64_t|double|const char \*)\s+(mpf3d_\w+)\s*\(", txt, re.M)
+            names += re.findall(r"^\s*(?:int|void|int64_t|double|const char \*)\s+(mpf[23]d_\w+)\s*\(", txt, re.M)
     return sorted(set(names))
 
 

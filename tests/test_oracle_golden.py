@@ -79,3 +79,48 @@ def test_unchecked_apt_reports_depth_overflow():
     mf = np.zeros((4, 3, 3, 3), np.int32)
     nf = np.zeros((3, 3, 3), np.int32)
     assert O.apt(phi, mf, nf, None, checked=False) == -1
+
+
+def _run2d_history(g):
+    f32 = bool(g["scalars_f32"])
+    sc = O.make_scalars(g["scalars"], f32)
+    phi, temp = g["phi0"].copy(), g["temp0"].copy()
+    N, nx, ny = phi.shape
+    mf = np.zeros((20, nx, ny), np.int32)
+    nf = np.zeros((nx, ny), np.int32)
+    phi_new = phi.copy()
+    for s in range(int(g["steps"])):
+        if float(g["cooling_rate"]) != 0.0:
+            O.temp_step(temp, float(g["cooling_rate"]), f32)
+        assert O.apt2d(phi, mf, nf) == 0
+        assert O.update2d(phi, phi_new, temp, mf, nf, g["wij"], g["aij"], g["mij"], g["n111"], sc) == 0
+        phi, phi_new = phi_new, phi
+        yield s, phi, nf, mf, temp
+
+
+@pytest.mark.parametrize("path", golden_files("run2d"), ids=golden_id)
+def test_oracle_2d_matches_reference_source(path):
+    """2D kernels (src/gpu_kernels.py): bit-exact phi, nf, mf and temperature
+    against the reference's own 2D source on every step."""
+    g = np.load(path)
+    for s, phi, nf, mf, temp in _run2d_history(g):
+        assert np.array_equal(phi, g["phi"][s]), f"phi differs at step {s}"
+        assert np.array_equal(nf, g["nf"][s]), f"nf differs at step {s}"
+        assert valid_mf_equal(mf, g["mf"][s], nf), f"mf differs at step {s}"
+        assert np.array_equal(temp, g["temp"][s]), f"temperature differs at step {s}"
+
+
+def test_oracle_2d_apt_wraps_x_and_clamps_y():
+    """2D APT boundaries: x periodic (a phase at x=0 activates x=nx-1), y
+    mirror (a phase at y=0 does not activate y=ny-1)."""
+    phi = np.zeros((3, 5, 4), np.float32)
+    phi[1, 0, 2] = 1.0
+    phi[2, 2, 0] = 1.0
+    phi[0] = 1.0 - phi[1:].sum(axis=0)
+    mf = np.zeros((20, 5, 4), np.int32)
+    nf = np.zeros((5, 4), np.int32)
+    assert O.apt2d(phi, mf, nf) == 0
+    active = lambda g, l, m: g in mf[: nf[l, m], l, m]
+    assert active(1, 4, 2) and active(1, 1, 2) and not active(1, 3, 2)
+    assert active(2, 2, 1) and not active(2, 2, 3)
+    assert O.apt2d(phi, np.zeros((1, 5, 4), np.int32), nf) == -1
