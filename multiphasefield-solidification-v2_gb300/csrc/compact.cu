@@ -360,19 +360,52 @@ __device__ __forceinline__ void interface_terms(const Params &P, const float3 (&
     b_sl = calc_b(P, F[0].cabs);
 }
 
+template <int S, int AMAX, bool HEAVY, int CAP>
+__device__ __forceinline__ void process_cell_cap(const In &in, const Out &out, const Mats &M, const Params &P,
+                                                 int32_t *__restrict__ err, int l, int m, int k);
+
+// Cells whose active list exceeds the fast capacity: the same update with
+// per-cell arrays sized for the full 2*slots active phases, kept out of line
+// so that their stack frame does not weigh on the common path.
+template <int S, int AMAX, bool HEAVY>
+__device__ __noinline__ void process_cell_wide(const In &in, const Out &out, const Mats &M, const Params &P,
+                                               int32_t *__restrict__ err, int l, int m, int k) {
+    process_cell_cap<S, AMAX, HEAVY, AMAX>(in, out, M, P, err, l, m, k);
+}
+
+// Active phases a cell holds in the fast path.  Grain boundaries, triple
+// junctions and interface cells keep 2-6; the per-cell arrays (ids, values,
+// Laplacians, pair sums) then stay small enough to live in L1.
+constexpr int FAST_CAP = 8;
+
 // Update of one cell whose neighbourhood is not uniform.  HEAVY enables the
 // anisotropic solid-liquid terms (cells with liquid and a solid active).
 template <int S, int AMAX, bool HEAVY>
 __device__ __forceinline__ void process_cell(const In &in, const Out &out, const Mats &M, const Params &P,
                                              int32_t *__restrict__ err, int l, int m, int k) {
+    process_cell_cap<S, AMAX, HEAVY, (AMAX < FAST_CAP ? AMAX : FAST_CAP)>(in, out, M, P, err, l, m, k);
+}
+
+// CAP: capacity of the per-cell arrays.  When the active list is longer
+// than CAP < AMAX the cell is redone by process_cell_wide; at CAP == AMAX an
+// overflow means more active phases than the slot template allows.
+template <int S, int AMAX, bool HEAVY, int CAP>
+__device__ __forceinline__ void process_cell_cap(const In &in, const Out &out, const Mats &M, const Params &P,
+                                                 int32_t *__restrict__ err, int l, int m, int k) {
     const uint32_t cells = P.cells32;
     const int lp = wrap_p(l, P.nx), lm = wrap_m(l, P.nx), mp = wrap_p(m, P.ny), mm = wrap_m(m, P.ny);
     const int kp = clamp_p(k, P.nz), km = clamp_m(k, P.nz);
     const uint32_t pt[7] = {cidx(P, l, m, k), cidx(P, lp, m, k), cidx(P, lm, m, k), cidx(P, l, mp, k),
                             cidx(P, l, mm, k), cidx(P, l, m, kp), cidx(P, l, m, km)};
     const uint32_t c = pt[0];
-    Active<AMAX> A;
-    gather<S, AMAX>(in, P, pt, A);
+    Active<CAP> A;
+    gather<S, CAP>(in, P, pt, A);
+    if constexpr (CAP < AMAX) {
+        if (A.ovf) {
+            process_cell_wide<S, AMAX, HEAVY>(in, out, M, P, err, l, m, k);
+            return;
+        }
+    }
     if (A.ovf) {
         // leave the cell as it was and report; the host re-runs the step with
         // a wider template
@@ -389,7 +422,7 @@ __device__ __forceinline__ void process_cell(const In &in, const Out &out, const
     const int n = A.n;
     const bool has_liq = n > 0 && A.ids[0] == LIQ;
     const bool has_solid = n > (has_liq ? 1 : 0);
-    float lap_sl[AMAX], b_sl[AMAX];
+    float lap_sl[CAP], b_sl[CAP];
     float w_sl = P.w0;
     lap_sl[0] = 0.0f;
     b_sl[0] = 1.0f;
@@ -457,7 +490,7 @@ __device__ __forceinline__ void process_cell(const In &in, const Out &out, const
     // reference splits into W_i - W_j (potential) plus either the
     // solid-liquid term of lap_sl or (A_i - A_j)/2 (gradient energy).
     const int N = P.N;
-    float W[AMAX], Ag[AMAX];
+    float W[CAP], Ag[CAP];
     for (int t1 = 0; t1 < n; ++t1) {
         const int i = A.ids[t1];
         float w = 0.0f, a = 0.0f;
@@ -472,7 +505,7 @@ __device__ __forceinline__ void process_cell(const In &in, const Out &out, const
     }
     const float dT = P.t_uniform ? P.dT_uniform : (float)(M.T0z[k] - P.Tmc);
     const float inv_n = 1.0f / (float)(n > 0 ? n : 1);
-    float outv[AMAX];
+    float outv[CAP];
     for (int t1 = 0; t1 < n; ++t1) {
         const int i = A.ids[t1];
         float dpi = 0.0f;
