@@ -192,6 +192,64 @@ int mpf3d_compact_to_dense_view(const uint32_t *head, const uint16_t *idx, const
                                 uint32_t stride, uint32_t base, int N, int nx, int ny, int nz, void *phi,
                                 int phi_dtype, void *stream);
 
+/* ---- observables, slices and checkpoints of a compact state -------------- */
+
+/* Reductions of compute_metrics_3d (tests/verification_3d.py:612-654) over
+ * the dense field the compact state stands for (unstored phases are 0). */
+typedef struct mpf3d_metrics {
+    double solid_sum;      /* sum over cells of 1 - phi_liquid */
+    double sum_err_max;    /* max over cells of |sum_g phi_g - 1| */
+    double phi_min;        /* min over every (phase, cell) entry */
+    double phi_max;        /* max over every (phase, cell) entry */
+    double front_sum;      /* sum of the column front heights (cells) */
+    double front_sq_sum;   /* sum of their squares */
+    double front_max;      /* highest column front */
+    int64_t nan_count;     /* NaN entries */
+    int64_t front_columns; /* columns holding solid above the threshold */
+    int32_t nf_max;        /* longest active-phase list (APT rule of kernel_update_nfmf_3d) */
+    int32_t reserved;
+} mpf3d_metrics;
+
+/* Metrics of one compact state into the device struct `result`; optional
+ * grain_sum (double[N], device) receives sum_cells phi_g for g >= 1 and
+ * front (float[ny][nx], device) the highest z whose solid fraction exceeds
+ * `threshold` per column, NaN where none (interface_positions_3d,
+ * tests/verification_3d.py:409-416). */
+int mpf3d_compact_metrics(const uint32_t *head, const uint16_t *idx, const float *val, int slots, int N,
+                          int nx, int ny, int nz, float threshold, mpf3d_metrics *result, double *grain_sum,
+                          float *front, void *stream);
+
+/* One 2D slice (axis 0: xy at z = index, 1: xz at y = index, 2: yz at x =
+ * index), row-major [W][H] with (W, H) = (nx, ny), (nx, nz) or (ny, nz):
+ * ids = argmax phase (first maximum, as numpy.argmax over the phase axis of
+ * save_phase_map_slice_3d, src/plot_utils_3d.py:36-72), vmax = its
+ * fraction, solid = 1 - phi_liquid (save_solid_slice,
+ * run_orientation_scan_3d.py:199-223).  Null outputs are skipped. */
+int mpf3d_compact_slice(const uint32_t *head, const uint16_t *idx, const float *val, int slots, int nx, int ny,
+                        int nz, int axis, int index, int32_t *ids, float *vmax, float *solid, void *stream);
+
+/* Checkpoints (no reference counterpart: the reference keeps no restart
+ * state).  A packed state is the head array plus the (id, value) entries of
+ * every cell that keeps values, cell-major, ascending ids; implicit single
+ * phases take no entry.  Offsets are recomputed from the heads, so head +
+ * entries is the whole checkpoint.  scratch: int64[mpf3d_compact_pack_scratch_len(cells)]. */
+int64_t mpf3d_compact_pack_scratch_len(int64_t cells);
+
+/* Writes the entry count to *total (device int64).  With ids_out/vals_out
+ * null only counts; otherwise writes entries that fit in `capacity`
+ * (entries past it set MPF3D_DEV_BAD_INPUT in *err). */
+int mpf3d_compact_pack(const uint32_t *head, const uint16_t *idx, const float *val, int slots, int64_t cells,
+                       int64_t *scratch, int64_t *total, uint16_t *ids_out, float *vals_out, int64_t capacity,
+                       int32_t *err, void *stream);
+
+/* Inverse of mpf3d_compact_pack into a state whose head array already holds
+ * the saved heads.  A cell with more entries than `slots` sets
+ * MPF3D_DEV_SLOT_OVERFLOW, entries past n_entries or a first id that
+ * disagrees with the head set MPF3D_DEV_BAD_INPUT. */
+int mpf3d_compact_unpack(const uint32_t *head, const uint16_t *ids_in, const float *vals_in, int64_t n_entries,
+                         int slots, int64_t cells, int64_t *scratch, uint16_t *idx_out, float *val_out, int32_t *err,
+                         void *stream);
+
 /* ---- batched instances (bicrystal / orientation-scan batches) -----------
  * No reference counterpart: the reference runs one domain at a time
  * (run_orientation_scan_3d.py:686-841, tests/verification_3d.py:1951-2011).
@@ -249,6 +307,24 @@ int mpf3d_batched_fronts(const uint32_t *head, const uint16_t *idx, const float 
 int mpf3d_batched_gb_rows(const uint32_t *head, const uint16_t *idx, const float *val, int slots,
                           const mpf3d_instance *inst, int n_inst, uint32_t total_cells, const int32_t *row_base,
                           double *gb, void *stream);
+
+/* Orientation-scan set-up: instance i holds a sphere of phase `solid_gid`
+ * of radius[i] cells centred at center[3i..3i+2] (cell units, index * dx is
+ * the position), liquid elsewhere, with the tanh profile of
+ * init_singlemode_sphere_3d (src/seed_modes_3d.py:59-113). */
+int mpf3d_batched_init_sphere(const mpf3d_instance *inst, int n_inst, uint32_t total_cells, double dx,
+                              double delta, const float *center, const float *radius, int solid_gid, int slots,
+                              uint32_t *head, uint16_t *idx, float *val, void *stream);
+
+/* Directional radii of measure_observables (run_orientation_scan_3d.py:
+ * 292-351): per instance i, direction d and sign (+, -), the distance in
+ * cells from center[3i..] along +-dirs[3d..] at which the trilinear
+ * interpolant of `phase` drops below `threshold`, marching in steps of
+ * step_cells; NaN where it does not.  out[(i*n_dir + d)*2 + sign]. */
+int mpf3d_batched_ray_radii(const uint32_t *head, const uint16_t *idx, const float *val, int slots,
+                            const mpf3d_instance *inst, int n_inst, uint32_t total_cells, int phase,
+                            const float *center, const float *dirs, int n_dir, double threshold, double step_cells,
+                            double *out, void *stream);
 
 /* ---- surrogate network kernels (BF16 tensor cores, FP32 accumulate) ------
  * No reference counterpart: the reference has no learned component.  BF16

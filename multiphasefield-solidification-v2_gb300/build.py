@@ -26,6 +26,7 @@ SOURCES = [
     ("dense_ref.cu", ["-fmad=false"]),
     ("dense2d.cu", ["-fmad=false"]),
     ("compact.cu", []),
+    ("observe.cu", []),
     ("mlp.cu", []),
 ]
 

@@ -28,13 +28,13 @@
 
 #include <mutex>
 
+#include "compact_state.cuh"
 #include "mpf3d.h"
 #include "mpf3d_internal.h"
 
 namespace mpf3d {
 namespace compact {
 
-constexpr int LIQ = 0;
 // the reference's pi approximation in the driving-force prefactor (:651)
 constexpr float FORCE_PREF = (float)(8.0 / 3.1415926535);
 
@@ -55,32 +55,6 @@ struct Params {
     float dT_uniform; // ... with T - T_melt = dT_uniform
 };
 
-struct In {
-    const uint32_t *__restrict__ head;
-    const uint16_t *__restrict__ idx;
-    const float *__restrict__ val;
-};
-struct Out {
-    uint32_t *__restrict__ head;
-    uint16_t *__restrict__ idx;
-    float *__restrict__ val;
-};
-
-__device__ __forceinline__ int hcount(uint32_t h) { return (int)(h & 0x7Fu); }
-__device__ __forceinline__ bool hexplicit(uint32_t h) { return (h & 0x80u) != 0u; }
-__device__ __forceinline__ int hid0(uint32_t h) { return (int)(h >> 8); }
-__device__ __forceinline__ uint32_t mkhead(int id0, int n, bool expl) {
-    return ((uint32_t)id0 << 8) | (expl ? 0x80u : 0u) | (uint32_t)n;
-}
-// value of stored entry 0 of a cell with head h
-__device__ __forceinline__ float value0(const In &in, uint32_t h, uint32_t q) {
-    return (hcount(h) >= 2 || hexplicit(h)) ? __ldg(in.val + q) : 1.0f;
-}
-
-__device__ __forceinline__ int wrap_p(int l, int n) { return l < n - 1 ? l + 1 : 0; }
-__device__ __forceinline__ int wrap_m(int l, int n) { return l > 0 ? l - 1 : n - 1; }
-__device__ __forceinline__ int clamp_p(int k, int n) { return k < n - 1 ? k + 1 : n - 1; }
-__device__ __forceinline__ int clamp_m(int k, int n) { return k > 0 ? k - 1 : 0; }
 
 __device__ __forceinline__ int64_t cell_of(const Params &P, int l, int m, int k) {
     return ((int64_t)k * P.ny + m) * P.nx + l;
@@ -755,33 +729,8 @@ __global__ void active_count_kernel(In in, int nx, int ny, int nz, int32_t *__re
     const int m = blockIdx.y * blockDim.y + threadIdx.y;
     const int l = blockIdx.z * blockDim.z + threadIdx.z;
     if (k >= nz || m >= ny || l >= nx) return;
-    const int64_t cells = (int64_t)nx * ny * nz;
-    const int lp = wrap_p(l, nx), lm = wrap_m(l, nx), mp = wrap_p(m, ny), mm = wrap_m(m, ny);
-    const int kp = clamp_p(k, nz), km = clamp_m(k, nz);
-    auto ci = [&](int a, int b, int d) { return ((int64_t)d * ny + b) * nx + a; };
-    const int64_t pt[7] = {ci(l, m, k), ci(lp, m, k), ci(lm, m, k), ci(l, mp, k),
-                           ci(l, mm, k), ci(l, m, kp), ci(l, m, km)};
-    auto id_at = [&](int p, int s) {
-        return s == 0 ? hid0(in.head[pt[p]]) : (int)in.idx[s * cells + pt[p]];
-    };
-    // count distinct ids of the 7 sorted lists by repeated minimum extraction
-    int pos[7];
-    for (int p = 0; p < 7; ++p) pos[p] = 0;
-    int n = 0, last = -1;
-    while (true) {
-        int best = 1 << 30;
-        for (int p = 0; p < 7; ++p) {
-            const int c = min(hcount(in.head[pt[p]]), S);
-            while (pos[p] < c && id_at(p, pos[p]) <= last) ++pos[p];
-            if (pos[p] < c) best = min(best, id_at(p, pos[p]));
-        }
-        if (best == (1 << 30)) break;
-        last = best;
-        ++n;
-    }
-    nf[((int64_t)l * ny + m) * nz + k] = n;
+    nf[((int64_t)l * ny + m) * nz + k] = active_count_at<S>(in, nx, ny, nz, l, m, k);
 }
-
 
 // ---------------------------------------------------------------------------
 // Batches of independent domains ("instances") sharing one set of state
@@ -884,18 +833,6 @@ __global__ void batched_init_bicrystal_kernel(Out out, const mpf3d_instance *__r
         }
         out.head[c] = mkhead(id0, n, n == 1 && v0 != 1.0f);
     }
-}
-
-// stored fraction of phase g at cell c (0 if not stored)
-template <int S>
-__device__ __forceinline__ float phase_at(const In &in, uint32_t stride, uint32_t c, int g) {
-    const uint32_t h = __ldg(in.head + c);
-    const int n = min(hcount(h), S);
-    if (n == 0) return 0.0f;
-    if (hid0(h) == g) return value0(in, h, c);
-    for (int s = 1; s < n; ++s)
-        if ((int)__ldg(in.idx + (size_t)s * stride + c) == g) return __ldg(in.val + (size_t)s * stride + c);
-    return 0.0f;
 }
 
 // Per instance: mean front height of each grain half (highest z with solid
@@ -1010,10 +947,6 @@ dim3 zfast_grid(int nx, int ny, int nz, dim3 b) {
     return dim3((nz + b.x - 1) / b.x, (ny + b.y - 1) / b.y, (nx + b.z - 1) / b.z);
 }
 
-bool dims_ok(int nx, int ny, int nz) {
-    return nx > 0 && ny > 0 && nz > 0 && nx <= 65535 * 32 && ny <= 65535 * 8 && nz <= 65535 * 8 &&
-           (int64_t)nx * ny * nz < ((int64_t)1 << 40);
-}
 
 template <int S, int AMAX>
 void launch_step(const In &in, const Out &out, const Mats &M, const Params &P, const Queue &Q, int parity,
@@ -1260,12 +1193,6 @@ Params shared_params(const mpf3d_scalars *sc, int enable_anisotropy, int enable_
     return P;
 }
 
-int sms_of_current_device() {
-    int dev = 0, sms = 148;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    return sms;
-}
 
 template <int S, int AMAX>
 void launch_batched(const In &in, const Out &out, const Mats &M, const Params &P0, const mpf3d_instance *inst,

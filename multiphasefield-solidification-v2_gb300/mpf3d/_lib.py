@@ -38,6 +38,17 @@ class Tuning(ctypes.Structure):
                 ("iface_blocks_per_sm", ctypes.c_int32), ("iface_threads", ctypes.c_int32)]
 
 
+class Metrics(ctypes.Structure):
+    """mpf3d_metrics: reductions of compute_metrics_3d over a compact state."""
+    _fields_ = [("solid_sum", ctypes.c_double), ("sum_err_max", ctypes.c_double), ("phi_min", ctypes.c_double),
+                ("phi_max", ctypes.c_double), ("front_sum", ctypes.c_double), ("front_sq_sum", ctypes.c_double),
+                ("front_max", ctypes.c_double), ("nan_count", ctypes.c_int64), ("front_columns", ctypes.c_int64),
+                ("nf_max", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+
+
+_F32 = ctypes.c_float
+_U32 = ctypes.c_uint32
+
 # name -> (restype, argtypes)
 _SIGS = {
     "mpf3d_version": (_I32, []),
@@ -50,6 +61,14 @@ _SIGS = {
     "mpf2d_dense_update": (_I32, [_VP, _VP, _I32, _VP, _I32, _VP, _I32, _VP, _VP, _VP, _VP, _VP,
                                   _I32, _I32, _I32, ctypes.POINTER(Scalars), _VP, _VP]),
     "mpf2d_dense_temp": (_I32, [_VP, _I32, _F64, _I32, _I32, _I32, _VP]),
+    "mpf3d_compact_metrics": (_I32, [_VP, _VP, _VP, _I32, _I32, _I32, _I32, _I32, _F32, _VP, _VP, _VP, _VP]),
+    "mpf3d_compact_slice": (_I32, [_VP, _VP, _VP, _I32, _I32, _I32, _I32, _I32, _I32, _VP, _VP, _VP, _VP]),
+    "mpf3d_compact_pack_scratch_len": (_I64, [_I64]),
+    "mpf3d_compact_pack": (_I32, [_VP, _VP, _VP, _I32, _I64, _VP, _VP, _VP, _VP, _I64, _VP, _VP]),
+    "mpf3d_compact_unpack": (_I32, [_VP, _VP, _VP, _I64, _I32, _I64, _VP, _VP, _VP, _VP, _VP]),
+    "mpf3d_batched_init_sphere": (_I32, [_VP, _I32, _U32, _F64, _F64, _VP, _VP, _I32, _I32, _VP, _VP, _VP, _VP]),
+    "mpf3d_batched_ray_radii": (_I32, [_VP, _VP, _VP, _I32, _VP, _I32, _U32, _I32, _VP, _VP, _I32, _F64, _F64,
+                                       _VP, _VP]),
     "mpf3d_compact_from_dense": (_I32, [_VP, _I32, _I32, _I32, _I32, _I32, _I32, _VP, _VP, _VP, _VP, _VP]),
     "mpf3d_compact_to_dense": (_I32, [_VP, _VP, _VP, _I32, _I32, _I32, _I32, _I32, _VP, _I32, _VP]),
     "mpf3d_compact_active_count": (_I32, [_VP, _VP, _I32, _I32, _I32, _I32, _VP, _VP]),

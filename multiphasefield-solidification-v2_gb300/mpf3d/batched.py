@@ -44,9 +44,16 @@ def _e2_flat(phys: Physics, delta_a: float) -> float:
 
 
 class BatchedBicrystals:
+    """A batch of independent domains stepped together.  layout="bicrystal"
+    (default): grain 1 | grain 2 over a base of `base_height` cells, liquid
+    above.  layout="sphere": a sphere of grain 1 with radius[i] cells centred
+    at center[i] (cells; default the box centre nx/2, ny/2, nz/2) in liquid,
+    the set-up of the reference's orientation scan (grain 2 stays absent)."""
+
     def __init__(self, dims, quats, undercooling, delta_a, phys: Physics | None = None, *,
                  base_height: float = 16.0, slots: int = 4, anisotropy: bool = True,
-                 torque: bool = True, device="cuda:0"):
+                 torque: bool = True, device="cuda:0", layout: str = "bicrystal", radius=None,
+                 center=None):
         import torch
 
         self.torch = torch
@@ -118,10 +125,31 @@ class BatchedBicrystals:
         self.step_count = 0
         self.graph = None
         h, i_, v = self.buf[0]
-        rc = _lib.lib().mpf3d_batched_init_bicrystal(self._ip(), n, self.total_cells, self.phys.dx,
-                                                     d["delta"], h.data_ptr(), i_.data_ptr(),
-                                                     v.data_ptr(), self.err.data_ptr(), self._stream())
-        _lib.check(rc, "batched_init_bicrystal")
+        self.layout = layout
+        if layout == "bicrystal":
+            rc = _lib.lib().mpf3d_batched_init_bicrystal(self._ip(), n, self.total_cells, self.phys.dx,
+                                                         d["delta"], h.data_ptr(), i_.data_ptr(),
+                                                         v.data_ptr(), self.err.data_ptr(), self._stream())
+            _lib.check(rc, "batched_init_bicrystal")
+        elif layout == "sphere":
+            if radius is None:
+                raise ValueError("layout='sphere' needs radius (cells, scalar or per instance)")
+            rad = np.array(np.broadcast_to(np.asarray(radius, np.float64), (n,)))
+            if center is None:
+                cen = np.array([[nx / 2.0, ny / 2.0, nz / 2.0] for nx, ny, nz in self.dims])
+            else:
+                cen = np.array(np.broadcast_to(np.asarray(center, np.float64), (n, 3)))
+            self.center_cells = np.ascontiguousarray(cen, np.float64)
+            self.radius_cells = np.ascontiguousarray(rad, np.float64)
+            self._center = torch.as_tensor(self.center_cells, dtype=torch.float32).to(self.device)
+            self._radius = torch.as_tensor(self.radius_cells, dtype=torch.float32).to(self.device)
+            rc = _lib.lib().mpf3d_batched_init_sphere(self._ip(), n, self.total_cells, self.phys.dx, d["delta"],
+                                                      self._center.data_ptr(), self._radius.data_ptr(), 1,
+                                                      self.slots, h.data_ptr(), i_.data_ptr(), v.data_ptr(),
+                                                      self._stream())
+            _lib.check(rc, "batched_init_sphere")
+        else:
+            raise ValueError(f"unknown layout {layout!r}")
         self.check()
 
     # -- plumbing ----------------------------------------------------------------
@@ -226,6 +254,36 @@ class BatchedBicrystals:
                 slope = np.polyfit(ks[sel], xs, 1)[0]
                 out[i] = math.degrees(math.atan(slope))
         return out
+
+    def ray_radii(self, dirs, threshold: float = 0.5, step_cells: float = 0.5, phase: int = 1,
+                  center=None) -> np.ndarray:
+        """directional_radius_symmetric (run_orientation_scan_3d.py:338-351)
+        of `phase` from each instance's centre along each direction: the mean
+        of the finite crossing distances (cells) along +d and -d, NaN if
+        neither crosses.  Returns [n_instances, n_dirs]."""
+        t = self.torch
+        dirs = np.ascontiguousarray(np.asarray(dirs, np.float64).reshape(-1, 3))
+        if center is None:
+            if not hasattr(self, "_center"):
+                raise ValueError("center is needed for layouts without a sphere centre")
+            cen = self._center
+        else:
+            cen = t.as_tensor(np.broadcast_to(np.asarray(center, np.float64), (self.n, 3)).copy(),
+                              dtype=t.float32).to(self.device)
+        dd = t.as_tensor(dirs, dtype=t.float32).to(self.device)
+        out = t.empty(self.n * len(dirs) * 2, dtype=t.float64, device=self.device)
+        h, i_, v = self.buf[self.cur]
+        rc = _lib.lib().mpf3d_batched_ray_radii(h.data_ptr(), i_.data_ptr(), v.data_ptr(), self.slots, self._ip(),
+                                                self.n, self.total_cells, int(phase), cen.data_ptr(), dd.data_ptr(),
+                                                len(dirs), float(threshold), float(step_cells), out.data_ptr(),
+                                                self._stream())
+        _lib.check(rc, "batched_ray_radii")
+        r = out.view(self.n, len(dirs), 2).cpu().numpy()
+        with np.errstate(invalid="ignore"):
+            fin = np.isfinite(r)
+            cnt = fin.sum(axis=2)
+            mean = np.where(fin, r, 0.0).sum(axis=2) / np.maximum(cnt, 1)
+        return np.where(cnt > 0, mean, np.nan)
 
     def dense(self, i: int, dtype=np.float32):
         """Dense phi [3, nx, ny, nz] of instance i (host)."""

@@ -94,20 +94,39 @@ class CompactSolver:
             if phi.dim() != 4 or phi.dtype not in (torch.float32, torch.float64):
                 raise ValueError("phi0 must be float32/float64 [N, nx, ny, nz]")
         self.N, self.nx, self.ny, self.nz = (int(s) for s in phi.shape)
+        if tuple(np.shape(aij)) != (self.N, self.N):
+            raise ValueError(f"aij must have shape {(self.N, self.N)}")
+        aij32 = np.asarray(aij, np.float32)
+        self._setup(slots, z_profile(temp0), wij, aij32 * aij32, mij, n111)
+        if owner_init is not None:
+            owner, slab, prof = owner_init
+            h, i_, v = self.buf[0]
+            rc = _lib.lib().mpf3d_compact_init_owner(owner.data_ptr(), slab, prof.data_ptr(), self.nx, self.ny,
+                                                     self.nz, self.slots, h.data_ptr(), i_.data_ptr(),
+                                                     v.data_ptr(), self._stream())
+            _lib.check(rc, "compact_init_owner")
+        else:
+            dphi = phi.to(self.device).contiguous()
+            self._from_dense(dphi)
+        self.check()
+
+    def _setup(self, slots, t0z, wij, a2ij, mij, n111):
+        """Device-side set-up shared by the constructors: matrices, scratch and
+        the two state buffers (contents undefined)."""
+        torch = _torch()
         self.cells = self.nx * self.ny * self.nz
         self.slots = slots
         self.amax = _SLOT_TEMPLATES[slots]
         to = lambda a, dt: torch.as_tensor(np.ascontiguousarray(a), dtype=dt).to(self.device)
-        self.T0z = to(z_profile(temp0), torch.float64)
+        self.T0z = to(t0z, torch.float64)
         if self.T0z.numel() != self.nz:
             raise ValueError("temperature profile length must equal nz")
-        for nm, a, shp in (("wij", wij, (self.N, self.N)), ("aij", aij, (self.N, self.N)),
+        for nm, a, shp in (("wij", wij, (self.N, self.N)), ("a2ij", a2ij, (self.N, self.N)),
                            ("mij", mij, (self.N, self.N)), ("n111", n111, (self.N, 8, 3))):
             if tuple(np.shape(a)) != shp:
                 raise ValueError(f"{nm} must have shape {shp}")
-        aij32 = np.asarray(aij, np.float32)
         self.wij = to(np.asarray(wij, np.float32), torch.float32)
-        self.a2ij = to(aij32 * aij32, torch.float32)
+        self.a2ij = to(np.asarray(a2ij, np.float32), torch.float32)
         self.mij = to(np.asarray(mij, np.float32), torch.float32)
         self.n111 = to(np.asarray(n111, np.float32), torch.float32)
         self.err = torch.zeros(1, dtype=torch.int32, device=self.device)
@@ -120,17 +139,6 @@ class CompactSolver:
         self.cur = 0
         self.step_count = 0
         self.tuning = None  # launch shape (mpf3d_tuning); None = library default
-        if owner_init is not None:
-            owner, slab, prof = owner_init
-            h, i_, v = self.buf[0]
-            rc = _lib.lib().mpf3d_compact_init_owner(owner.data_ptr(), slab, prof.data_ptr(), self.nx, self.ny,
-                                                     self.nz, self.slots, h.data_ptr(), i_.data_ptr(),
-                                                     v.data_ptr(), self._stream())
-            _lib.check(rc, "compact_init_owner")
-        else:
-            dphi = phi.to(self.device).contiguous()
-            self._from_dense(dphi)
-        self.check()
 
     @classmethod
     def from_owner(cls, owner, profile, temp0, n111, wij, aij, mij, phys: Physics | None = None, **kw):
@@ -277,3 +285,36 @@ class CompactSolver:
 
     def state_bytes(self) -> int:
         return self.cells * (4 + 6 * self.slots)
+
+    # -- observables and checkpoints (computed on the GPU, see mpf3d.observe) ----
+    def metrics(self, threshold: float = 0.5, runtime_s: float = 0.0) -> dict:
+        """compute_metrics_3d (tests/verification_3d.py:612-654) of the current state."""
+        from . import observe
+
+        return observe.metrics(self, threshold=threshold, runtime_s=runtime_s)
+
+    def interface_positions(self, threshold: float = 0.5) -> np.ndarray:
+        """interface_positions_3d (tests/verification_3d.py:409-416): [nx, ny] float64, NaN where no solid."""
+        from . import observe
+
+        return observe.interface_positions(self, threshold=threshold)
+
+    def phase_slice(self, axis: str = "xy", index=None) -> dict:
+        """Argmax phase ids, their fractions and the solid fraction of one slice."""
+        from . import observe
+
+        return observe.phase_slice(self, axis=axis, index=index)
+
+    def save(self, path: str) -> dict:
+        """Write a checkpoint (.npz) of the state and everything a resume needs."""
+        from . import observe
+
+        return observe.save_checkpoint(self, path)
+
+    @classmethod
+    def load(cls, path: str, device="cuda:0", slots=None) -> "CompactSolver":
+        """Resume from a checkpoint written by `save`; the next step continues
+        the run exactly."""
+        from . import observe
+
+        return observe.load_checkpoint(cls, path, device=device, slots=slots)
