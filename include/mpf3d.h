@@ -175,16 +175,29 @@ typedef struct mpf3d_tuning {
 } mpf3d_tuning;
 
 /* mpf3d_compact_step with an explicit launch shape (NULL: the default
- * {4, 8, 8, 256, 8, 128}), as chosen by the package's autotuner.  No
- * reference counterpart: the reference launches a fixed [4, 4, 4] block
- * (config_3d.yaml gpu.threads_per_block). */
+ * {4, 8, 8, 256, 8, 128}), as chosen by the package's autotuner, and
+ * optional quiet-tile flags.  No reference counterpart: the reference
+ * launches a fixed [4, 4, 4] block (config_3d.yaml gpu.threads_per_block)
+ * over every cell.
+ *
+ * tile_flags (uint8, mpf3d_compact_tile_flags_len bytes, or NULL): per
+ * 32 x 1 x sweep_zb tile of the sweep, "every cell was uniform" for the last
+ * two steps (alternating halves by parity).  A tile that was uniform with
+ * its 6 neighbours in the previous step is skipped -- no reads, no writes:
+ * the output buffer already holds its cells.  The result is identical to
+ * tile_flags = NULL.  Zero the whole array whenever the state buffers are
+ * written other than by this function (initialisation, restore, rollback)
+ * or sweep_zb changes; steps must alternate parity. */
 int mpf3d_compact_step_tuned(const uint32_t *head, const uint16_t *idx, const float *val, uint32_t *head_out,
                              uint16_t *idx_out, float *val_out, int slots, int amax, const double *T0z,
                              double Tm_plus_cool, const float *wij, const float *a2ij, const float *mij,
                              const float *n111, int N, int nx, int ny, int nz, const mpf3d_scalars *scalars,
                              int enable_anisotropy, int enable_torque, int symmetric_normals,
                              uint32_t *work_items, uint32_t *work_count, int parity, int32_t *err,
-                             void *stream, const mpf3d_tuning *tuning);
+                             void *stream, const mpf3d_tuning *tuning, uint8_t *tile_flags);
+
+/* Bytes of tile_flags for an nx x ny x nz domain (any sweep_zb). */
+int64_t mpf3d_compact_tile_flags_len(int nx, int ny, int nz);
 
 /* compact state -> dense phi of one domain stored at cells [base, base +
  * nx*ny*nz) of state arrays whose slot planes are `stride` cells apart. */

@@ -44,7 +44,7 @@ struct Params {
     uint32_t cells32;
     float e2_flat, b_flat;  // eps^2 and b for a liquid gradient below the floor
     float inv_dx2, inv_2dx, half_over_dx, inv_dx, dt;
-    float eps0, eps0sq, w0, mu_a, delta_a, mu_da, pp, tan_a0, g2_floor, ksi, theta_c, Sf;
+    float eps0, eps0sq, w0, mu_a, delta_a, mu_da, pp, tan_a0, g2_floor, ksi, theta_c, cos_theta_lo, Sf;
     double Tmc;  // T_melt + accumulated cooling (float64)
     int use_aniso, use_torque;
     int sym_normals;  // every grain's n111 rows 4..7 are -(rows 3..0)
@@ -99,6 +99,31 @@ __device__ __forceinline__ Facet facet(float3 g, const float *__restrict__ u, fl
     return sym ? facet_n<4>(g, u, g2_floor) : facet_n<8>(g, u, g2_floor);
 }
 
+// facet_n over normals already held in registers (a grain's normals are
+// loaded once per cell and reused at the 7 stencil points)
+template <int NT>
+__device__ __forceinline__ Facet facet_regs(float3 g, const float (&u)[24], float g2_floor) {
+    Facet f;
+    f.q = g.x * g.x + g.y * g.y + g.z * g.z;
+    f.valid = !(f.q < g2_floor);
+    f.cabs = 0.0f; f.cs = 0.0f; f.nx = 1.0f; f.ny = 0.0f; f.nz = 0.0f;
+    if (!f.valid) return f;
+    float ig = rsqrtf(f.q);
+    float gx = g.x * ig, gy = g.y * ig, gz = g.z * ig;
+#pragma unroll
+    for (int t = 0; t < NT; ++t) {
+        const float ux = u[3 * t], uy = u[3 * t + 1], uz = u[3 * t + 2];
+        float d = gx * ux + gy * uy + gz * uz;
+        float a = fabsf(d);
+        if (a > f.cabs) {
+            f.cabs = a; f.cs = d; f.nx = ux; f.ny = uy; f.nz = uz;
+        }
+    }
+    f.cabs = fminf(f.cabs, 1.0f);
+    f.cs = fminf(fmaxf(f.cs, -1.0f), 1.0f);
+    return f;
+}
+
 // a(theta) (calc_a_from_cos :24-30)
 __device__ __forceinline__ float calc_a(const Params &P, float c) {
     float c2 = c * c;
@@ -110,6 +135,7 @@ __device__ __forceinline__ float calc_a(const Params &P, float c) {
 // b(theta) (calc_b_from_cos :33-55)
 __device__ __forceinline__ float calc_b(const Params &P, float c) {
     c = fminf(fmaxf(c, -1.0f), 1.0f);
+    if (c <= P.cos_theta_lo) return 1.0f;  // theta >= theta_c: outside the cusp
     float theta = acosf(c);
     if (theta >= P.theta_c) return 1.0f;
     const float hp = 1.57079632679489662f;
@@ -274,14 +300,15 @@ __device__ __forceinline__ PointTerms point_terms(const Params &P, float3 g, con
 // a cell from the liquid gradient at the 7 points and the liquid's second
 // derivatives at the cell (aniso_term1_solid_3d :149-204, torque_A11_3d
 // :386-441, A13_divergence_3d :344-383, calc_b_from_cos :33-55).
+template <int NT>
 __device__ __forceinline__ void interface_terms(const Params &P, const float3 (&G)[7], const float (&vL)[7],
-                                                const float (&h2)[6], const float *__restrict__ u, bool torque,
+                                                const float (&h2)[6], const float (&u)[24], bool torque,
                                                 float &lap_sl, float &b_sl) {
     Facet F[7];
     bool any = false;
 #pragma unroll
     for (int p = 0; p < 7; ++p) {
-        F[p] = facet(G[p], u, P.g2_floor, P.sym_normals != 0);
+        F[p] = facet_regs<NT>(G[p], u, P.g2_floor);
         any = any || F[p].valid;
     }
     const float Lc = vL[0];
@@ -334,52 +361,19 @@ __device__ __forceinline__ void interface_terms(const Params &P, const float3 (&
     b_sl = calc_b(P, F[0].cabs);
 }
 
-template <int S, int AMAX, bool HEAVY, int CAP>
-__device__ __forceinline__ void process_cell_cap(const In &in, const Out &out, const Mats &M, const Params &P,
-                                                 int32_t *__restrict__ err, int l, int m, int k);
-
-// Cells whose active list exceeds the fast capacity: the same update with
-// per-cell arrays sized for the full 2*slots active phases, kept out of line
-// so that their stack frame does not weigh on the common path.
-template <int S, int AMAX, bool HEAVY>
-__device__ __noinline__ void process_cell_wide(const In &in, const Out &out, const Mats &M, const Params &P,
-                                               int32_t *__restrict__ err, int l, int m, int k) {
-    process_cell_cap<S, AMAX, HEAVY, AMAX>(in, out, M, P, err, l, m, k);
-}
-
-// Active phases a cell holds in the fast path.  Grain boundaries, triple
-// junctions and interface cells keep 2-6; the per-cell arrays (ids, values,
-// Laplacians, pair sums) then stay small enough to live in L1.
-constexpr int FAST_CAP = 8;
-
 // Update of one cell whose neighbourhood is not uniform.  HEAVY enables the
 // anisotropic solid-liquid terms (cells with liquid and a solid active).
 template <int S, int AMAX, bool HEAVY>
 __device__ __forceinline__ void process_cell(const In &in, const Out &out, const Mats &M, const Params &P,
                                              int32_t *__restrict__ err, int l, int m, int k) {
-    process_cell_cap<S, AMAX, HEAVY, (AMAX < FAST_CAP ? AMAX : FAST_CAP)>(in, out, M, P, err, l, m, k);
-}
-
-// CAP: capacity of the per-cell arrays.  When the active list is longer
-// than CAP < AMAX the cell is redone by process_cell_wide; at CAP == AMAX an
-// overflow means more active phases than the slot template allows.
-template <int S, int AMAX, bool HEAVY, int CAP>
-__device__ __forceinline__ void process_cell_cap(const In &in, const Out &out, const Mats &M, const Params &P,
-                                                 int32_t *__restrict__ err, int l, int m, int k) {
     const uint32_t cells = P.cells32;
     const int lp = wrap_p(l, P.nx), lm = wrap_m(l, P.nx), mp = wrap_p(m, P.ny), mm = wrap_m(m, P.ny);
     const int kp = clamp_p(k, P.nz), km = clamp_m(k, P.nz);
     const uint32_t pt[7] = {cidx(P, l, m, k), cidx(P, lp, m, k), cidx(P, lm, m, k), cidx(P, l, mp, k),
                             cidx(P, l, mm, k), cidx(P, l, m, kp), cidx(P, l, m, km)};
     const uint32_t c = pt[0];
-    Active<CAP> A;
-    gather<S, CAP>(in, P, pt, A);
-    if constexpr (CAP < AMAX) {
-        if (A.ovf) {
-            process_cell_wide<S, AMAX, HEAVY>(in, out, M, P, err, l, m, k);
-            return;
-        }
-    }
+    Active<AMAX> A;
+    gather<S, AMAX>(in, P, pt, A);
     if (A.ovf) {
         // leave the cell as it was and report; the host re-runs the step with
         // a wider template
@@ -396,7 +390,7 @@ __device__ __forceinline__ void process_cell_cap(const In &in, const Out &out, c
     const int n = A.n;
     const bool has_liq = n > 0 && A.ids[0] == LIQ;
     const bool has_solid = n > (has_liq ? 1 : 0);
-    float lap_sl[CAP], b_sl[CAP];
+    float lap_sl[AMAX], b_sl[AMAX];
     float w_sl = P.w0;
     lap_sl[0] = 0.0f;
     b_sl[0] = 1.0f;
@@ -437,9 +431,19 @@ __device__ __forceinline__ void process_cell_cap(const In &in, const Out &out, c
             h2[3] = (Lxpyp - Lxpym - Lxmyp + Lxmym) * qq;
             h2[4] = (Lxpzp - Lxpzm - Lxmzp + Lxmzm) * qq;
             h2[5] = (Lypzp - Lypzm - Lymzp + Lymzm) * qq;
-            for (int t = 1; t < n; ++t)
-                interface_terms(P, G, A.vL, h2, M.n111 + (size_t)(P.n111_base + A.ids[t]) * 24, P.use_torque != 0,
-                                lap_sl[t], b_sl[t]);
+            for (int t = 1; t < n; ++t) {
+                const float *ug = M.n111 + (size_t)(P.n111_base + A.ids[t]) * 24;
+                float un[24];
+                if (P.sym_normals) {
+#pragma unroll
+                    for (int q = 0; q < 12; ++q) un[q] = __ldg(ug + q);
+                    interface_terms<4>(P, G, A.vL, h2, un, P.use_torque != 0, lap_sl[t], b_sl[t]);
+                } else {
+#pragma unroll
+                    for (int q = 0; q < 24; ++q) un[q] = __ldg(ug + q);
+                    interface_terms<8>(P, G, A.vL, h2, un, P.use_torque != 0, lap_sl[t], b_sl[t]);
+                }
+            }
             if (A.ts > 0) {
                 const Facet fs = facet(A.gs, M.n111 + (size_t)(P.n111_base + A.ids[A.ts]) * 24, P.g2_floor,
                                        P.sym_normals != 0);
@@ -464,7 +468,7 @@ __device__ __forceinline__ void process_cell_cap(const In &in, const Out &out, c
     // reference splits into W_i - W_j (potential) plus either the
     // solid-liquid term of lap_sl or (A_i - A_j)/2 (gradient energy).
     const int N = P.N;
-    float W[CAP], Ag[CAP];
+    float W[AMAX], Ag[AMAX];
     for (int t1 = 0; t1 < n; ++t1) {
         const int i = A.ids[t1];
         float w = 0.0f, a = 0.0f;
@@ -479,7 +483,7 @@ __device__ __forceinline__ void process_cell_cap(const In &in, const Out &out, c
     }
     const float dT = P.t_uniform ? P.dT_uniform : (float)(M.T0z[k] - P.Tmc);
     const float inv_n = 1.0f / (float)(n > 0 ? n : 1);
-    float outv[CAP];
+    float outv[AMAX];
     for (int t1 = 0; t1 < n; ++t1) {
         const int i = A.ids[t1];
         float dpi = 0.0f;
@@ -567,9 +571,11 @@ __device__ __forceinline__ void push(const Queue &Q, int parity, bool want, bool
 
 constexpr int SWEEP_ZB = 4;  // cells per thread along z (default; batches always use it)
 
-// The sweep of one column of ZB cells (l, m, k0..k0+ZB-1) of a domain.
+// The sweep of one column of ZB cells (l, m, k0..k0+ZB-1) of a domain;
+// returns whether every one of them was uniform (cells past the top count
+// as uniform).
 template <int ZB = SWEEP_ZB>
-__device__ __forceinline__ void sweep_column(const In &in, const Out &out, const Params &P, const Queue &Q, int parity,
+__device__ __forceinline__ bool sweep_column(const In &in, const Out &out, const Params &P, const Queue &Q, int parity,
                                              int l, int m, int k0) {
     const uint32_t plane = (uint32_t)P.nx * (uint32_t)P.ny;
     const uint32_t col = P.base + (uint32_t)m * (uint32_t)P.nx + (uint32_t)l;
@@ -579,6 +585,7 @@ __device__ __forceinline__ void sweep_column(const In &in, const Out &out, const
     const uint32_t dym = (m > 0) ? (uint32_t)(-P.nx) : (uint32_t)((P.ny - 1) * P.nx);
     // heads of the column k0-1 .. k0+ZB (z clamped)
     uint32_t hz[ZB + 2];
+    bool all_uniform = true;
 #pragma unroll
     for (int j = 0; j < ZB + 2; ++j) {
         const int kk = min(max(k0 - 1 + j, 0), P.nz - 1);
@@ -612,24 +619,67 @@ __device__ __forceinline__ void sweep_column(const In &in, const Out &out, const
             // the one phase of the neighbourhood keeps the cell at exactly 1
             out.head[c] = h0;
         } else {
+            all_uniform = false;
             const bool heavy = liq && sol && P.use_aniso;
             push(Q, parity, heavy, true, P.cells32, c);
             push(Q, parity, !heavy, false, P.cells32, c);
         }
     }
+    return all_uniform;
+}
+
+// Quiet tiles.  A tile is the 32 x 1 x ZB cells one warp of the sweep
+// covers.  When every cell of a tile is uniform in step n, step n leaves the
+// tile unchanged (S(n+1) = S(n) there).  If the tile and its 6 face
+// neighbours were all uniform in step n-1, the neighbourhoods of the tile's
+// cells are unchanged in step n, so the tile is uniform again, and its
+// content in the output buffer -- written by step n-2, i.e. S(n-1) -- already
+// equals S(n+1): the warp writes nothing and queues nothing.  flags[2][tiles]
+// (one byte per tile, uniform = 1) alternate with the step parity; both
+// halves must be zero after the state buffers are written from outside the
+// step (the first step then visits every tile).
+struct Tiles {
+    uint8_t *__restrict__ flags;
+    int ntx, nkb;
+    uint32_t n;  // tiles per parity half
+};
+
+template <int ZB>
+__host__ __device__ __forceinline__ uint32_t tiles_of(int nx, int ny, int nz) {
+    return (uint32_t)((nz + ZB - 1) / ZB) * (uint32_t)ny * (uint32_t)((nx + 31) / 32);
 }
 
 template <int S, int AMAX, int ZB = SWEEP_ZB>
 __global__ void __launch_bounds__(512) sweep_kernel(In in, Out out, Mats M, Params P, Queue Q, int parity,
-                                                    int32_t *__restrict__ err) {
+                                                    Tiles T, int32_t *__restrict__ err) {
     const int l = blockIdx.x * blockDim.x + threadIdx.x;
     const int m = blockIdx.y * blockDim.y + threadIdx.y;
     const int k0 = (blockIdx.z * blockDim.z + threadIdx.z) * ZB;
     if (blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.x < 2 && threadIdx.y == 0 &&
         threadIdx.z == 0)
         Q.count[2 * (parity ^ 1) + threadIdx.x] = 0;  // the previous step's kernels are done with them
-    if (l >= P.nx || m >= P.ny || k0 >= P.nz) return;
-    sweep_column<ZB>(in, out, P, Q, parity, l, m, k0);
+    // a warp is one threadIdx.y row: its 32 lanes share m and k0
+    if (m >= P.ny || k0 >= P.nz) return;
+    if (!T.flags) {
+        if (l < P.nx) sweep_column<ZB>(in, out, P, Q, parity, l, m, k0);
+        return;
+    }
+    const int tx = (int)blockIdx.x, kb = k0 / ZB;
+    const uint8_t *fin = T.flags + (size_t)(parity ^ 1) * T.n;
+    uint8_t *fout = T.flags + (size_t)parity * T.n;
+    auto tid = [&](int a, int b, int c) { return ((uint32_t)c * (uint32_t)P.ny + (uint32_t)b) * (uint32_t)T.ntx + a; };
+    const uint32_t t = tid(tx, m, kb);
+    const bool quiet = fin[t] && fin[tid(tx + 1 < T.ntx ? tx + 1 : 0, m, kb)] && fin[tid(tx > 0 ? tx - 1 : T.ntx - 1, m, kb)] &&
+                       fin[tid(tx, m + 1 < P.ny ? m + 1 : 0, kb)] && fin[tid(tx, m > 0 ? m - 1 : P.ny - 1, kb)] &&
+                       fin[tid(tx, m, kb + 1 < T.nkb ? kb + 1 : kb)] && fin[tid(tx, m, kb > 0 ? kb - 1 : kb)];
+    const bool lane0 = (threadIdx.x & 31) == 0;
+    if (quiet) {
+        if (lane0) fout[t] = 1;
+        return;
+    }
+    const bool uni = l < P.nx ? sweep_column<ZB>(in, out, P, Q, parity, l, m, k0) : true;
+    const bool all = __all_sync(0xffffffffu, uni);
+    if (lane0) fout[t] = all ? 1 : 0;
 }
 
 // Kernel 2 of a step: the cells queued for the general update, one thread
@@ -652,7 +702,7 @@ __global__ void __launch_bounds__(256) general_kernel(In in, Out out, Mats M, Pa
 // Kernel 3 of a step: the queued solid-liquid interface cells, one thread
 // per cell, all lanes of a warp on the same (heavy) path.
 template <int S, int AMAX>
-__global__ void __launch_bounds__(128, 4) interface_kernel(In in, Out out, Mats M, Params P, Queue Q, int parity,
+__global__ void __launch_bounds__(128, 5) interface_kernel(In in, Out out, Mats M, Params P, Queue Q, int parity,
                                                            int32_t *__restrict__ err) {
     const uint32_t n = *(volatile uint32_t *)(Q.count + 2 * parity + 1);
     const uint32_t plane = (uint32_t)P.nx * (uint32_t)P.ny;
@@ -950,12 +1000,13 @@ dim3 zfast_grid(int nx, int ny, int nz, dim3 b) {
 
 template <int S, int AMAX>
 void launch_step(const In &in, const Out &out, const Mats &M, const Params &P, const Queue &Q, int parity,
-                 int32_t *err, cudaStream_t s, const mpf3d_tuning &T) {
+                 uint8_t *tile_flags, int32_t *err, cudaStream_t s, const mpf3d_tuning &T) {
     const int by = T.sweep_by;
     dim3 blk(32, by, 1);
-#define SWEEP_LAUNCH(ZB)                                                                                        \
-    sweep_kernel<S, AMAX, ZB><<<dim3((P.nx + 31) / 32, (P.ny + by - 1) / by, (P.nz + ZB - 1) / ZB), blk, 0, s>>>( \
-        in, out, M, P, Q, parity, err)
+#define SWEEP_LAUNCH(ZB)                                                                                           \
+    sweep_kernel<S, AMAX, ZB><<<dim3((P.nx + 31) / 32, (P.ny + by - 1) / by, (P.nz + ZB - 1) / ZB), blk, 0, s>>>(    \
+        in, out, M, P, Q, parity,                                                                                  \
+        Tiles{tile_flags, (P.nx + 31) / 32, (P.nz + ZB - 1) / ZB, tiles_of<ZB>(P.nx, P.ny, P.nz)}, err)
     if (T.sweep_zb == 2) SWEEP_LAUNCH(2);
     else if (T.sweep_zb == 8) SWEEP_LAUNCH(8);
     else SWEEP_LAUNCH(4);
@@ -1037,116 +1088,6 @@ extern "C" int mpf3d_compact_active_count(const uint32_t *cnt, const uint16_t *i
     return cudaGetLastError() == cudaSuccess ? MPF3D_OK : MPF3D_ERR_CUDA;
 }
 
-extern "C" int mpf3d_compact_step_tuned(const uint32_t *cnt, const uint16_t *idx, const float *val,
-                                        uint32_t *cnt_out, uint16_t *idx_out, float *val_out, int slots, int amax,
-                                        const double *T0z, double Tm_plus_cool, const float *wij, const float *a2ij,
-                                        const float *mij, const float *n111, int N, int nx, int ny, int nz,
-                                        const mpf3d_scalars *sc, int enable_anisotropy, int enable_torque,
-                                        int symmetric_normals, uint32_t *work_items, uint32_t *work_count,
-                                        int parity, int32_t *err, void *stream, const mpf3d_tuning *tuning) {
-    const mpf3d_tuning T = tuning ? *tuning : kDefaultTuning;
-    if (!tuning_ok(T)) return MPF3D_ERR_ARG;
-    if (!cnt || !idx || !val || !cnt_out || !idx_out || !val_out || !T0z || !wij || !a2ij || !mij || !n111 || !sc ||
-        !err || !work_items || !work_count)
-        return MPF3D_ERR_ARG;
-    if (N <= 0 || N > 65535 || !dims_ok(nx, ny, nz)) return MPF3D_ERR_ARG;
-    if ((int64_t)nx * ny * nz >= ((int64_t)1 << 31)) return MPF3D_ERR_TOO_LARGE;
-    if (cnt == cnt_out || idx == idx_out || val == val_out) return MPF3D_ERR_ARG;
-    const double *v = sc->v;
-    Params P;
-    P.nx = nx; P.ny = ny; P.nz = nz; P.N = N;
-    P.cells = (int64_t)nx * ny * nz;
-    const double dx = v[MPF3D_S_DX];
-    P.inv_dx2 = (float)(1.0 / (dx * dx));
-    P.inv_2dx = (float)(1.0 / (2.0 * dx));
-    P.half_over_dx = (float)(0.5 / dx);
-    P.inv_dx = (float)(1.0 / dx);
-    P.dt = (float)v[MPF3D_S_DT];
-    P.eps0 = (float)v[MPF3D_S_EPS0_SL];
-    P.eps0sq = (float)(v[MPF3D_S_EPS0_SL] * v[MPF3D_S_EPS0_SL]);
-    P.w0 = (float)v[MPF3D_S_W0_SL];
-    P.mu_a = (float)v[MPF3D_S_MU_A];
-    P.delta_a = (float)v[MPF3D_S_DELTA_A];
-    P.mu_da = (float)(v[MPF3D_S_MU_A] * v[MPF3D_S_DELTA_A]);
-    P.pp = (float)(v[MPF3D_S_P_ROUND] * v[MPF3D_S_P_ROUND]);
-    P.tan_a0 = (float)tan(v[MPF3D_S_A0]);
-    P.g2_floor = (float)v[MPF3D_S_G2_FLOOR];
-    P.ksi = (float)v[MPF3D_S_KSI];
-    P.theta_c = (float)v[MPF3D_S_THETA_C_RAD];
-    P.Sf = (float)v[MPF3D_S_SF];
-    P.Tmc = Tm_plus_cool;
-    P.use_aniso = enable_anisotropy != 0;
-    P.use_torque = enable_anisotropy != 0 && enable_torque != 0;
-    P.cells32 = (uint32_t)P.cells;
-    P.sym_normals = symmetric_normals != 0;
-    P.base = 0;
-    P.n111_base = 0;
-    P.t_uniform = 0;
-    P.dT_uniform = 0.0f;
-    {
-        // a(0) and b(0): the values for a gradient below g2_floor
-        const double pp = v[MPF3D_S_P_ROUND] * v[MPF3D_S_P_ROUND];
-        const double a_flat = v[MPF3D_S_MU_A] * (1.0 + v[MPF3D_S_DELTA_A] * (sqrt(pp) + tan(v[MPF3D_S_A0]) * sqrt(1.0 + pp)));
-        const double e = v[MPF3D_S_EPS0_SL] * a_flat;
-        P.e2_flat = (float)(e * e);
-        const double th = acos(0.0), thc = v[MPF3D_S_THETA_C_RAD];
-        double b = 1.0;
-        if (th < thc) {
-            double y = 0.5 * 3.14159265358979323846 * (th / thc);
-            y = fmin(fmax(y, 1e-6), 0.5 * 3.14159265358979323846 - 1e-6);
-            const double t = tan(y);
-            b = v[MPF3D_S_KSI] + (1.0 - v[MPF3D_S_KSI]) * t * tanh(1.0 / t);
-        }
-        P.b_flat = (float)b;
-    }
-    In in{cnt, idx, val};
-    Out out{cnt_out, idx_out, val_out};
-    Mats M{T0z, wij, a2ij, mij, n111};
-    Queue Q{work_items, work_count};
-    parity &= 1;
-    cudaStream_t s = (cudaStream_t)stream;
-    if (slots == 4 && amax == 8) launch_step<4, 8>(in, out, M, P, Q, parity, err, s, T);
-    else if (slots == 8 && amax == 16) launch_step<8, 16>(in, out, M, P, Q, parity, err, s, T);
-    else if (slots == 16 && amax == 32) launch_step<16, 32>(in, out, M, P, Q, parity, err, s, T);
-    else return MPF3D_ERR_ARG;
-    return cudaGetLastError() == cudaSuccess ? MPF3D_OK : MPF3D_ERR_CUDA;
-}
-
-extern "C" int mpf3d_compact_step(const uint32_t *cnt, const uint16_t *idx, const float *val, uint32_t *cnt_out,
-                                  uint16_t *idx_out, float *val_out, int slots, int amax, const double *T0z,
-                                  double Tm_plus_cool, const float *wij, const float *a2ij, const float *mij,
-                                  const float *n111, int N, int nx, int ny, int nz, const mpf3d_scalars *sc,
-                                  int enable_anisotropy, int enable_torque, int symmetric_normals,
-                                  uint32_t *work_items, uint32_t *work_count, int parity, int32_t *err,
-                                  void *stream) {
-    return mpf3d_compact_step_tuned(cnt, idx, val, cnt_out, idx_out, val_out, slots, amax, T0z, Tm_plus_cool, wij,
-                                    a2ij, mij, n111, N, nx, ny, nz, sc, enable_anisotropy, enable_torque,
-                                    symmetric_normals, work_items, work_count, parity, err, stream, nullptr);
-}
-
-extern "C" int mpf3d_compact_to_dense_view(const uint32_t *head, const uint16_t *idx, const float *val, int slots,
-                                           uint32_t stride, uint32_t base, int N, int nx, int ny, int nz, void *phi,
-                                           int phi_dtype, void *stream) {
-    if (!phi || !head || !idx || !val || N <= 0 || N > 65535 || !dims_ok(nx, ny, nz)) return MPF3D_ERR_ARG;
-    if ((uint64_t)base + (uint64_t)nx * ny * nz > (uint64_t)stride) return MPF3D_ERR_ARG;
-    cudaStream_t s = (cudaStream_t)stream;
-    dim3 b(32, 4, 2);
-    dim3 g = zfast_grid(nx, ny, nz, b);
-    In in{head, idx, val};
-#define TDV(T, SS) to_dense_kernel<T, SS><<<g, b, 0, s>>>(in, N, nx, ny, nz, stride, base, (T *)phi)
-    if (phi_dtype == MPF3D_F32) {
-        if (slots == 4) TDV(float, 4); else if (slots == 8) TDV(float, 8); else if (slots == 16) TDV(float, 16);
-        else return MPF3D_ERR_ARG;
-    } else if (phi_dtype == MPF3D_F64) {
-        if (slots == 4) TDV(double, 4); else if (slots == 8) TDV(double, 8); else if (slots == 16) TDV(double, 16);
-        else return MPF3D_ERR_ARG;
-    } else {
-        return MPF3D_ERR_DTYPE;
-    }
-#undef TDV
-    return cudaGetLastError() == cudaSuccess ? MPF3D_OK : MPF3D_ERR_CUDA;
-}
-
 namespace {
 
 // physics shared by every cell of a step, from the 13 kernel scalars
@@ -1171,6 +1112,9 @@ Params shared_params(const mpf3d_scalars *sc, int enable_anisotropy, int enable_
     P.g2_floor = (float)v[MPF3D_S_G2_FLOOR];
     P.ksi = (float)v[MPF3D_S_KSI];
     P.theta_c = (float)v[MPF3D_S_THETA_C_RAD];
+    // below this cosine acosf(c) >= theta_c holds with margin (acosf is
+    // within a few ulp; the margin is ~1e-5 rad), so b = 1 without acosf
+    P.cos_theta_lo = (float)(cos(v[MPF3D_S_THETA_C_RAD]) - 1.0e-5);
     P.Sf = (float)v[MPF3D_S_SF];
     P.Tmc = v[MPF3D_S_T_MELT];
     P.use_aniso = enable_anisotropy != 0;
@@ -1205,6 +1149,82 @@ void launch_batched(const In &in, const Out &out, const Mats &M, const Params &P
 }
 
 }  // namespace
+
+extern "C" int mpf3d_compact_step_tuned(const uint32_t *cnt, const uint16_t *idx, const float *val,
+                                        uint32_t *cnt_out, uint16_t *idx_out, float *val_out, int slots, int amax,
+                                        const double *T0z, double Tm_plus_cool, const float *wij, const float *a2ij,
+                                        const float *mij, const float *n111, int N, int nx, int ny, int nz,
+                                        const mpf3d_scalars *sc, int enable_anisotropy, int enable_torque,
+                                        int symmetric_normals, uint32_t *work_items, uint32_t *work_count,
+                                        int parity, int32_t *err, void *stream, const mpf3d_tuning *tuning,
+                                        uint8_t *tile_flags) {
+    const mpf3d_tuning T = tuning ? *tuning : kDefaultTuning;
+    if (!tuning_ok(T)) return MPF3D_ERR_ARG;
+    if (!cnt || !idx || !val || !cnt_out || !idx_out || !val_out || !T0z || !wij || !a2ij || !mij || !n111 || !sc ||
+        !err || !work_items || !work_count)
+        return MPF3D_ERR_ARG;
+    if (N <= 0 || N > 65535 || !dims_ok(nx, ny, nz)) return MPF3D_ERR_ARG;
+    if ((int64_t)nx * ny * nz >= ((int64_t)1 << 31)) return MPF3D_ERR_TOO_LARGE;
+    if (cnt == cnt_out || idx == idx_out || val == val_out) return MPF3D_ERR_ARG;
+    Params P = shared_params(sc, enable_anisotropy, enable_torque, symmetric_normals);
+    P.nx = nx; P.ny = ny; P.nz = nz; P.N = N;
+    P.cells = (int64_t)nx * ny * nz;
+    P.cells32 = (uint32_t)P.cells;
+    P.Tmc = Tm_plus_cool;
+    In in{cnt, idx, val};
+    Out out{cnt_out, idx_out, val_out};
+    Mats M{T0z, wij, a2ij, mij, n111};
+    Queue Q{work_items, work_count};
+    parity &= 1;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (slots == 4 && amax == 8) launch_step<4, 8>(in, out, M, P, Q, parity, tile_flags, err, s, T);
+    else if (slots == 8 && amax == 16) launch_step<8, 16>(in, out, M, P, Q, parity, tile_flags, err, s, T);
+    else if (slots == 16 && amax == 32) launch_step<16, 32>(in, out, M, P, Q, parity, tile_flags, err, s, T);
+    else return MPF3D_ERR_ARG;
+    return cudaGetLastError() == cudaSuccess ? MPF3D_OK : MPF3D_ERR_CUDA;
+}
+
+extern "C" int mpf3d_compact_step(const uint32_t *cnt, const uint16_t *idx, const float *val, uint32_t *cnt_out,
+                                  uint16_t *idx_out, float *val_out, int slots, int amax, const double *T0z,
+                                  double Tm_plus_cool, const float *wij, const float *a2ij, const float *mij,
+                                  const float *n111, int N, int nx, int ny, int nz, const mpf3d_scalars *sc,
+                                  int enable_anisotropy, int enable_torque, int symmetric_normals,
+                                  uint32_t *work_items, uint32_t *work_count, int parity, int32_t *err,
+                                  void *stream) {
+    return mpf3d_compact_step_tuned(cnt, idx, val, cnt_out, idx_out, val_out, slots, amax, T0z, Tm_plus_cool, wij,
+                                    a2ij, mij, n111, N, nx, ny, nz, sc, enable_anisotropy, enable_torque,
+                                    symmetric_normals, work_items, work_count, parity, err, stream, nullptr,
+                                    nullptr);
+}
+
+extern "C" int64_t mpf3d_compact_tile_flags_len(int nx, int ny, int nz) {
+    if (!dims_ok(nx, ny, nz)) return 0;
+    return 2 * (int64_t)tiles_of<2>(nx, ny, nz);
+}
+
+extern "C" int mpf3d_compact_to_dense_view(const uint32_t *head, const uint16_t *idx, const float *val, int slots,
+                                           uint32_t stride, uint32_t base, int N, int nx, int ny, int nz, void *phi,
+                                           int phi_dtype, void *stream) {
+    if (!phi || !head || !idx || !val || N <= 0 || N > 65535 || !dims_ok(nx, ny, nz)) return MPF3D_ERR_ARG;
+    if ((uint64_t)base + (uint64_t)nx * ny * nz > (uint64_t)stride) return MPF3D_ERR_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    dim3 b(32, 4, 2);
+    dim3 g = zfast_grid(nx, ny, nz, b);
+    In in{head, idx, val};
+#define TDV(T, SS) to_dense_kernel<T, SS><<<g, b, 0, s>>>(in, N, nx, ny, nz, stride, base, (T *)phi)
+    if (phi_dtype == MPF3D_F32) {
+        if (slots == 4) TDV(float, 4); else if (slots == 8) TDV(float, 8); else if (slots == 16) TDV(float, 16);
+        else return MPF3D_ERR_ARG;
+    } else if (phi_dtype == MPF3D_F64) {
+        if (slots == 4) TDV(double, 4); else if (slots == 8) TDV(double, 8); else if (slots == 16) TDV(double, 16);
+        else return MPF3D_ERR_ARG;
+    } else {
+        return MPF3D_ERR_DTYPE;
+    }
+#undef TDV
+    return cudaGetLastError() == cudaSuccess ? MPF3D_OK : MPF3D_ERR_CUDA;
+}
+
 
 extern "C" int mpf3d_batched_init_bicrystal(const mpf3d_instance *inst, int n_inst, uint32_t total_cells, double dx,
                                             double delta, uint32_t *head, uint16_t *idx, float *val, int32_t *err,

@@ -94,7 +94,8 @@ _SIGS = {
     "mpf3d_f32_to_bf16": (_I32, [_VP, _VP, _I64, _VP]),
     "mpf3d_compact_step_tuned": (_I32, [_VP, _VP, _VP, _VP, _VP, _VP, _I32, _I32, _VP, _F64, _VP, _VP, _VP, _VP,
                                         _I32, _I32, _I32, _I32, ctypes.POINTER(Scalars), _I32, _I32, _I32,
-                                        _VP, _VP, _I32, _VP, _VP, ctypes.POINTER(Tuning)]),
+                                        _VP, _VP, _I32, _VP, _VP, ctypes.POINTER(Tuning), _VP]),
+    "mpf3d_compact_tile_flags_len": (_I64, [_I32, _I32, _I32]),
     "mpf3d_compact_step_noalloc": (_I32, [_VP, _VP, _VP, _VP, _VP, _VP, _I32, _I32, _VP, _F64, _VP, _VP,
                                           _VP, _VP, _I32, _I32, _I32, _I32, ctypes.POINTER(Scalars),
                                           _I32, _I32, _I32, _VP, _VP]),
@@ -107,13 +108,20 @@ class LibraryMissing(RuntimeError):
     pass
 
 
+def library_path() -> str:
+    """The library to load: $MPF3D_LIBRARY when set (another build of the
+    same C ABI), else the in-tree build next to this module."""
+    return os.environ.get("MPF3D_LIBRARY") or LIB_PATH
+
+
 def lib():
     global _LIB
     if _LIB is None:
-        if not os.path.exists(LIB_PATH):
-            raise LibraryMissing(f"{LIB_PATH} is not built: run `python -c \"import __graft_entry__ as g; "
+        path = library_path()
+        if not os.path.exists(path):
+            raise LibraryMissing(f"{path} is not built: run `python -c \"import __graft_entry__ as g; "
                                  "g.build()\"` (or multiphasefield-solidification-v2_gb300/build.py)")
-        L = ctypes.CDLL(LIB_PATH)
+        L = ctypes.CDLL(path)
         for name, (res, args) in _SIGS.items():
             fn = getattr(L, name)
             fn.restype = res

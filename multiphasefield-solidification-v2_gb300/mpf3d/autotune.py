@@ -70,6 +70,7 @@ def time_config(solver, cfg, steps: int) -> float:
     cur, count = solver.cur, solver.step_count
     prev = solver.tuning
     solver.tuning = make(cfg)
+    solver.forget_history()  # the trial starts from the snapshot, not from the last step
     stream = torch.cuda.current_stream(solver.device)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     try:
@@ -85,7 +86,7 @@ def time_config(solver, cfg, steps: int) -> float:
         solver.cur, solver.step_count = cur, count
         for dst, src in zip(solver.buf[cur], snap):
             dst.copy_(src)
-        solver.work_count.zero_()
+        solver.forget_history()
     return ms
 
 

@@ -139,6 +139,19 @@ class CompactSolver:
         self.cur = 0
         self.step_count = 0
         self.tuning = None  # launch shape (mpf3d_tuning); None = library default
+        # quiet-tile flags of the sweep (see mpf3d_compact_step_tuned)
+        self.skip_quiet_tiles = True
+        n_flags = int(_lib.lib().mpf3d_compact_tile_flags_len(self.nx, self.ny, self.nz))
+        self.tile_flags = torch.zeros(max(n_flags, 1), dtype=torch.uint8, device=self.device)
+        self._tiles_zb = None
+
+    def forget_history(self) -> None:
+        """Clear what the step keeps from earlier steps -- the quiet-tile flags
+        and the work-list counters.  Required after the state buffers are
+        written other than by a step (restore, rollback); the next step then
+        visits every tile."""
+        self.tile_flags.zero_()
+        self.work_count.zero_()
 
     @classmethod
     def from_owner(cls, owner, profile, temp0, n111, wij, aij, mij, phys: Physics | None = None, **kw):
@@ -180,6 +193,10 @@ class CompactSolver:
         src = self.buf[self.cur]
         dst = self.buf[1 - self.cur]
         tmc = self.T_melt + step_index * self.cooling_rate
+        zb = self.tuning.sweep_zb if self.tuning is not None else 4
+        if zb != self._tiles_zb:  # the tile geometry follows the sweep shape
+            self.tile_flags.zero_()
+            self._tiles_zb = zb
         rc = _lib.lib().mpf3d_compact_step_tuned(
             src[0].data_ptr(), src[1].data_ptr(), src[2].data_ptr(), dst[0].data_ptr(),
             dst[1].data_ptr(), dst[2].data_ptr(), self.slots, self.amax, self.T0z.data_ptr(), tmc,
@@ -187,7 +204,8 @@ class CompactSolver:
             self.N, self.nx, self.ny, self.nz, ctypes.byref(self.scalars), int(self.anisotropy),
             int(self.torque), int(self.symmetric_normals), self.work_items.data_ptr(),
             self.work_count.data_ptr(), step_index & 1, self.err.data_ptr(), self._stream(),
-            ctypes.byref(self.tuning) if self.tuning is not None else None)
+            ctypes.byref(self.tuning) if self.tuning is not None else None,
+            self.tile_flags.data_ptr() if self.skip_quiet_tiles else None)
         _lib.check(rc, "compact_step")
         self.cur = 1 - self.cur
 
@@ -224,12 +242,12 @@ class CompactSolver:
         self.amax = _SLOT_TEMPLATES[self.slots]
         self.buf = [self._alloc(), self._alloc()]
         self.cur = 0
-        self.work_count.zero_()
         c2, i2, v2 = self.buf[0]
         c2.copy_(cnt)
         i2[: old * self.cells].copy_(idx)
         v2[: old * self.cells].copy_(val)
         self.step_count = steps
+        self.forget_history()
 
     def autotune(self, steps: int = 8, use_cache: bool = True) -> dict:
         """Pick the fastest launch shape for this problem (see mpf3d.autotune)."""

@@ -135,3 +135,38 @@ def test_every_launch_shape_gives_the_same_state(tmp_path, monkeypatch):
     s.step(4)
     assert np.array_equal(s.to_dense(), want)
     assert (tmp_path / "tuning.json").exists()
+
+
+@pytest.mark.parametrize("cfg", [None, (2, 16, 32, 128, 32, 64), (8, 4, 8, 256, 8, 128)])
+def test_quiet_tile_skipping_changes_nothing(cfg):
+    """Skipping tiles that stayed uniform (with their neighbours) gives the
+    same state, bit for bit, as visiting every cell: over a moving front,
+    across a launch-shape change in the middle of the run and after a
+    restore from a snapshot."""
+    from mpf3d import autotune, inputs
+    case = inputs.voronoi_case(72, 20, 64, 6, 10, seed=21, orientation_seed=3, undercooling=1.5)
+    a = make_solver(case)
+    b = make_solver(case)
+    b.skip_quiet_tiles = False
+    if cfg is not None:
+        a.tuning = autotune.make(cfg)
+        b.tuning = autotune.make(cfg)
+    quiet_seen = 0.0
+    for chunk in range(6):
+        a.step(10)
+        b.step(10)
+        assert np.array_equal(a.to_dense(), b.to_dense()), f"after {10 * (chunk + 1)} steps"
+        n = int(a.tile_flags.numel())
+        quiet_seen = max(quiet_seen, float(a.tile_flags.float().sum().item()) / n)
+        if chunk == 2:  # a shape change in the middle resets the tile history
+            a.tuning = autotune.make((4, 8, 8, 256, 8, 128) if cfg is None else (2, 8, 16, 128, 16, 64))
+    assert quiet_seen > 0.2  # most of the liquid is skipped
+    snap = [t.clone() for t in a.buf[a.cur]]
+    a.step(5)
+    for dst, src in zip(a.buf[a.cur], snap):  # writing the state from outside ...
+        dst.copy_(src)
+    a.forget_history()  # ... requires forgetting the step history
+    a.step_count -= 5
+    b.step(5)
+    a.step(5)
+    assert np.array_equal(a.to_dense(), b.to_dense())
