@@ -187,14 +187,21 @@ typedef struct mpf3d_tuning {
  * the output buffer already holds its cells.  The result is identical to
  * tile_flags = NULL.  Zero the whole array whenever the state buffers are
  * written other than by this function (initialisation, restore, rollback)
- * or sweep_zb changes; steps must alternate parity. */
+ * or sweep_zb changes; steps must alternate parity.  options: 0 or
+ * MPF3D_STEP_MULTI_LIST. */
 int mpf3d_compact_step_tuned(const uint32_t *head, const uint16_t *idx, const float *val, uint32_t *head_out,
                              uint16_t *idx_out, float *val_out, int slots, int amax, const double *T0z,
                              double Tm_plus_cool, const float *wij, const float *a2ij, const float *mij,
                              const float *n111, int N, int nx, int ny, int nz, const mpf3d_scalars *scalars,
                              int enable_anisotropy, int enable_torque, int symmetric_normals,
                              uint32_t *work_items, uint32_t *work_count, int parity, int32_t *err,
-                             void *stream, const mpf3d_tuning *tuning, uint8_t *tile_flags);
+                             void *stream, const mpf3d_tuning *tuning, uint8_t *tile_flags, int options);
+
+/* options of mpf3d_compact_step_tuned */
+#define MPF3D_STEP_MULTI_LIST 1 /* interface cells whose neighbourhood holds two or more solids (judged
+                                 * from the heads) get a work list of their own at
+                                 * work_items[cells .. 2*cells): work_items must then hold 2*cells
+                                 * entries and work_count 6.  Same results, fewer idle lanes. */
 
 /* Bytes of tile_flags for an nx x ny x nz domain (any sweep_zb). */
 int64_t mpf3d_compact_tile_flags_len(int nx, int ny, int nz);

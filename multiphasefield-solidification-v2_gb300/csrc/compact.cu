@@ -168,6 +168,11 @@ __device__ __forceinline__ float4 da_dgrad(const Params &P, float3 g, const Face
 struct Queue {
     uint32_t *__restrict__ items;
     uint32_t *__restrict__ count;
+    // With split set, interface cells whose active list holds two or more
+    // solids go to a third list at items[cells + ...] (counters count[4 +
+    // parity]): their warps loop over the solids, and keeping them apart
+    // from the one-solid majority spares those warps the idle iterations.
+    int split;
 };
 
 struct Mats {
@@ -554,18 +559,19 @@ __device__ __forceinline__ void process_cell(const In &in, const Out &out, const
 // (liquid and a solid in the neighbourhood, anisotropy on) to the back,
 // the rest (grain boundaries, junctions without liquid, the isotropic model)
 // to the front -- so that the general update runs with converged warps.
-__device__ __forceinline__ void push(const Queue &Q, int parity, bool want, bool back, uint32_t cells, uint32_t c) {
+__device__ __forceinline__ void push(const Queue &Q, int parity, bool want, int list, uint32_t cells, uint32_t c) {
     const unsigned am = __activemask();
     const unsigned bm = __ballot_sync(am, want);
     if (!bm) return;
     const int lane = threadIdx.x & 31;
     const int leader = __ffs(bm) - 1;
     uint32_t base = 0;
-    if (lane == leader) base = atomicAdd(Q.count + 2 * parity + (back ? 1 : 0), (uint32_t)__popc(bm));
+    uint32_t *ctr = list == 2 ? Q.count + 4 + parity : Q.count + 2 * parity + list;
+    if (lane == leader) base = atomicAdd(ctr, (uint32_t)__popc(bm));
     base = __shfl_sync(am, base, leader);
     if (want) {
         const uint32_t pos = base + __popc(bm & ((1u << lane) - 1u));
-        Q.items[back ? cells - 1u - pos : pos] = c;
+        Q.items[list == 0 ? pos : (list == 1 ? cells - 1u - pos : cells + pos)] = c;
     }
 }
 
@@ -621,8 +627,25 @@ __device__ __forceinline__ bool sweep_column(const In &in, const Out &out, const
         } else {
             all_uniform = false;
             const bool heavy = liq && sol && P.use_aniso;
-            push(Q, parity, heavy, true, P.cells32, c);
-            push(Q, parity, !heavy, false, P.cells32, c);
+            bool multi = false;
+            if (heavy && Q.split) {
+                // several solids in the active list: a head with 3+ phases or
+                // two solids, or two different solid first ids
+                int sid = -1;
+                const uint32_t hs[7] = {h0, hn[0], hn[1], hn[2], hn[3], hn[4], hn[5]};
+#pragma unroll
+                for (int p = 0; p < 7; ++p) {
+                    const int cn = hcount(hs[p]), id = hid0(hs[p]);
+                    if (cn >= 3 || (cn == 2 && id != LIQ)) multi = true;
+                    else if (cn >= 1 && id != LIQ) {
+                        if (sid < 0) sid = id;
+                        else if (sid != id) multi = true;
+                    }
+                }
+            }
+            push(Q, parity, heavy && !multi, 1, P.cells32, c);
+            push(Q, parity, heavy && multi, 2, P.cells32, c);
+            push(Q, parity, !heavy, 0, P.cells32, c);
         }
     }
     return all_uniform;
@@ -658,6 +681,9 @@ __global__ void __launch_bounds__(512) sweep_kernel(In in, Out out, Mats M, Para
     if (blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.x < 2 && threadIdx.y == 0 &&
         threadIdx.z == 0)
         Q.count[2 * (parity ^ 1) + threadIdx.x] = 0;  // the previous step's kernels are done with them
+    if (blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.x == 2 && threadIdx.y == 0 &&
+        threadIdx.z == 0 && Q.split)
+        Q.count[4 + (parity ^ 1)] = 0;
     // a warp is one threadIdx.y row: its 32 lanes share m and k0
     if (m >= P.ny || k0 >= P.nz) return;
     if (!T.flags) {
@@ -704,10 +730,11 @@ __global__ void __launch_bounds__(256) general_kernel(In in, Out out, Mats M, Pa
 template <int S, int AMAX>
 __global__ void __launch_bounds__(128, 5) interface_kernel(In in, Out out, Mats M, Params P, Queue Q, int parity,
                                                            int32_t *__restrict__ err) {
-    const uint32_t n = *(volatile uint32_t *)(Q.count + 2 * parity + 1);
+    const uint32_t na = *(volatile uint32_t *)(Q.count + 2 * parity + 1);
+    const uint32_t n = na + (Q.split ? *(volatile uint32_t *)(Q.count + 4 + parity) : 0u);
     const uint32_t plane = (uint32_t)P.nx * (uint32_t)P.ny;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const uint32_t c = Q.items[P.cells32 - 1u - i];
+        const uint32_t c = i < na ? Q.items[P.cells32 - 1u - i] : Q.items[P.cells32 + (i - na)];
         const int k = (int)(c / plane);
         const uint32_t r = c - (uint32_t)k * plane;
         const int m = (int)(r / (uint32_t)P.nx);
@@ -1157,7 +1184,7 @@ extern "C" int mpf3d_compact_step_tuned(const uint32_t *cnt, const uint16_t *idx
                                         const mpf3d_scalars *sc, int enable_anisotropy, int enable_torque,
                                         int symmetric_normals, uint32_t *work_items, uint32_t *work_count,
                                         int parity, int32_t *err, void *stream, const mpf3d_tuning *tuning,
-                                        uint8_t *tile_flags) {
+                                        uint8_t *tile_flags, int options) {
     const mpf3d_tuning T = tuning ? *tuning : kDefaultTuning;
     if (!tuning_ok(T)) return MPF3D_ERR_ARG;
     if (!cnt || !idx || !val || !cnt_out || !idx_out || !val_out || !T0z || !wij || !a2ij || !mij || !n111 || !sc ||
@@ -1174,7 +1201,7 @@ extern "C" int mpf3d_compact_step_tuned(const uint32_t *cnt, const uint16_t *idx
     In in{cnt, idx, val};
     Out out{cnt_out, idx_out, val_out};
     Mats M{T0z, wij, a2ij, mij, n111};
-    Queue Q{work_items, work_count};
+    Queue Q{work_items, work_count, (options & MPF3D_STEP_MULTI_LIST) ? 1 : 0};
     parity &= 1;
     cudaStream_t s = (cudaStream_t)stream;
     if (slots == 4 && amax == 8) launch_step<4, 8>(in, out, M, P, Q, parity, tile_flags, err, s, T);
@@ -1194,7 +1221,7 @@ extern "C" int mpf3d_compact_step(const uint32_t *cnt, const uint16_t *idx, cons
     return mpf3d_compact_step_tuned(cnt, idx, val, cnt_out, idx_out, val_out, slots, amax, T0z, Tm_plus_cool, wij,
                                     a2ij, mij, n111, N, nx, ny, nz, sc, enable_anisotropy, enable_torque,
                                     symmetric_normals, work_items, work_count, parity, err, stream, nullptr,
-                                    nullptr);
+                                    nullptr, 0);
 }
 
 extern "C" int64_t mpf3d_compact_tile_flags_len(int nx, int ny, int nz) {
@@ -1258,7 +1285,7 @@ extern "C" int mpf3d_batched_step(const uint32_t *head, const uint16_t *idx, con
     In in{head, idx, val};
     Out out{head_out, idx_out, val_out};
     Mats M{nullptr, wij, a2ij, mij, n111};
-    Queue Q{work_items, work_count};
+    Queue Q{work_items, work_count, 0};
     cudaStream_t s = (cudaStream_t)stream;
     parity &= 1;
     if (slots == 4 && amax == 8) launch_batched<4, 8>(in, out, M, P0, inst, n_inst, n_tiles, Q, parity, err, s);

@@ -12,6 +12,7 @@ import os
 LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libmpf3d.so")
 
 MPF3D_OK = 0
+STEP_MULTI_LIST = 1  # MPF3D_STEP_MULTI_LIST
 ERRORS = {-1: "bad argument", -2: "bad dtype", -3: "CUDA launch/call failed", -4: "size above limit"}
 
 DEV_BITS = {1: "unchecked APT needed more rows than mf has (MPF3D_DEV_MF_DEPTH)",
@@ -94,7 +95,7 @@ _SIGS = {
     "mpf3d_f32_to_bf16": (_I32, [_VP, _VP, _I64, _VP]),
     "mpf3d_compact_step_tuned": (_I32, [_VP, _VP, _VP, _VP, _VP, _VP, _I32, _I32, _VP, _F64, _VP, _VP, _VP, _VP,
                                         _I32, _I32, _I32, _I32, ctypes.POINTER(Scalars), _I32, _I32, _I32,
-                                        _VP, _VP, _I32, _VP, _VP, ctypes.POINTER(Tuning), _VP]),
+                                        _VP, _VP, _I32, _VP, _VP, ctypes.POINTER(Tuning), _VP, _I32]),
     "mpf3d_compact_tile_flags_len": (_I64, [_I32, _I32, _I32]),
     "mpf3d_compact_step_noalloc": (_I32, [_VP, _VP, _VP, _VP, _VP, _VP, _I32, _I32, _VP, _F64, _VP, _VP,
                                           _VP, _VP, _I32, _I32, _I32, _I32, ctypes.POINTER(Scalars),

@@ -130,9 +130,9 @@ class CompactSolver:
         self.mij = to(np.asarray(mij, np.float32), torch.float32)
         self.n111 = to(np.asarray(n111, np.float32), torch.float32)
         self.err = torch.zeros(1, dtype=torch.int32, device=self.device)
-        # scratch of the step: interface work list and its two counters
-        self.work_items = torch.empty(self.cells, dtype=torch.int32, device=self.device)
-        self.work_count = torch.zeros(4, dtype=torch.int32, device=self.device)
+        # scratch of the step: the three work lists (MPF3D_STEP_MULTI_LIST) and their counters
+        self.work_items = torch.empty(2 * self.cells, dtype=torch.int32, device=self.device)
+        self.work_count = torch.zeros(6, dtype=torch.int32, device=self.device)
         n111_np = np.asarray(n111, np.float32)
         self.symmetric_normals = bool(np.array_equal(n111_np[:, 4:8], -n111_np[:, [3, 2, 1, 0]]))
         self.buf = [self._alloc(), self._alloc()]
@@ -205,7 +205,7 @@ class CompactSolver:
             int(self.torque), int(self.symmetric_normals), self.work_items.data_ptr(),
             self.work_count.data_ptr(), step_index & 1, self.err.data_ptr(), self._stream(),
             ctypes.byref(self.tuning) if self.tuning is not None else None,
-            self.tile_flags.data_ptr() if self.skip_quiet_tiles else None)
+            self.tile_flags.data_ptr() if self.skip_quiet_tiles else None, _lib.STEP_MULTI_LIST)
         _lib.check(rc, "compact_step")
         self.cur = 1 - self.cur
 
