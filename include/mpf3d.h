@@ -302,13 +302,14 @@ int mpf3d_batched_init_bicrystal(const mpf3d_instance *inst, int n_inst, uint32_
 /* One step of every instance: the three step kernels of mpf3d_compact_step
  * launched once over the whole batch.  n_tiles = total sweep tiles.  Shared
  * physics from `scalars` (delta_a there is ignored); the rest as
- * mpf3d_compact_step with total_cells in place of nx*ny*nz. */
+ * mpf3d_compact_step_tuned with total_cells in place of nx*ny*nz (options:
+ * 0 or MPF3D_STEP_MULTI_LIST). */
 int mpf3d_batched_step(const uint32_t *head, const uint16_t *idx, const float *val, uint32_t *head_out,
                        uint16_t *idx_out, float *val_out, int slots, int amax, const mpf3d_instance *inst,
                        int n_inst, int n_tiles, uint32_t total_cells, const float *wij, const float *a2ij,
                        const float *mij, const float *n111, int N, const mpf3d_scalars *scalars,
                        int enable_anisotropy, int enable_torque, int symmetric_normals, uint32_t *work_items,
-                       uint32_t *work_count, int parity, int32_t *err, void *stream);
+                       uint32_t *work_count, int parity, int32_t *err, void *stream, int options);
 
 /* Observables per instance, accumulated into zeroed float64 arrays:
  * acc[6*i..6*i+5] = {sum of front heights left of split, columns left, sum

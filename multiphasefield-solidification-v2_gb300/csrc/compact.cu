@@ -851,6 +851,7 @@ __global__ void __launch_bounds__(256) batched_sweep_kernel(In in, Out out, Para
                                                             const mpf3d_instance *__restrict__ inst, int n_inst,
                                                             Queue Q, int parity) {
     if (blockIdx.x == 0 && threadIdx.x < 2 && threadIdx.y == 0) Q.count[2 * (parity ^ 1) + threadIdx.x] = 0;
+    if (blockIdx.x == 0 && threadIdx.x == 2 && threadIdx.y == 0 && Q.split) Q.count[4 + (parity ^ 1)] = 0;
     const int i = find_instance_by_tile(inst, n_inst, (int)blockIdx.x);
     const mpf3d_instance I = inst[i];
     const int t = (int)blockIdx.x - I.tile_start;
@@ -868,9 +869,10 @@ __global__ void __launch_bounds__(HEAVY ? 128 : 256) batched_queue_kernel(In in,
                                                                           const mpf3d_instance *__restrict__ inst,
                                                                           int n_inst, Queue Q, int parity,
                                                                           int32_t *__restrict__ err) {
-    const uint32_t n = *(volatile uint32_t *)(Q.count + 2 * parity + (HEAVY ? 1 : 0));
+    const uint32_t na = *(volatile uint32_t *)(Q.count + 2 * parity + (HEAVY ? 1 : 0));
+    const uint32_t n = na + ((HEAVY && Q.split) ? *(volatile uint32_t *)(Q.count + 4 + parity) : 0u);
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const uint32_t c = HEAVY ? Q.items[P0.cells32 - 1u - i] : Q.items[i];
+        const uint32_t c = !HEAVY ? Q.items[i] : (i < na ? Q.items[P0.cells32 - 1u - i] : Q.items[P0.cells32 + (i - na)]);
         const mpf3d_instance I = inst[find_instance_by_cell(inst, n_inst, c)];
         const Params P = instance_params(P0, I);
         const uint32_t r0 = c - I.offset;
@@ -1271,7 +1273,7 @@ extern "C" int mpf3d_batched_step(const uint32_t *head, const uint16_t *idx, con
                                   const float *mij, const float *n111, int N, const mpf3d_scalars *sc,
                                   int enable_anisotropy, int enable_torque, int symmetric_normals,
                                   uint32_t *work_items, uint32_t *work_count, int parity, int32_t *err,
-                                  void *stream) {
+                                  void *stream, int options) {
     if (!head || !idx || !val || !head_out || !idx_out || !val_out || !inst || !wij || !a2ij || !mij || !n111 ||
         !sc || !err || !work_items || !work_count || n_inst <= 0 || n_tiles <= 0 || total_cells == 0 || N <= 0 ||
         N > 65535)
@@ -1285,7 +1287,7 @@ extern "C" int mpf3d_batched_step(const uint32_t *head, const uint16_t *idx, con
     In in{head, idx, val};
     Out out{head_out, idx_out, val_out};
     Mats M{nullptr, wij, a2ij, mij, n111};
-    Queue Q{work_items, work_count, 0};
+    Queue Q{work_items, work_count, (options & MPF3D_STEP_MULTI_LIST) ? 1 : 0};
     cudaStream_t s = (cudaStream_t)stream;
     parity &= 1;
     if (slots == 4 && amax == 8) launch_batched<4, 8>(in, out, M, P0, inst, n_inst, n_tiles, Q, parity, err, s);

@@ -118,8 +118,9 @@ class BatchedBicrystals:
         for k, v in enumerate(self.phys.kernel_scalars(f32=False)):
             self.scalars.v[k] = float(v)
         self.err = torch.zeros(1, dtype=torch.int32, device=self.device)
-        self.work_items = torch.empty(self.total_cells, dtype=torch.int32, device=self.device)
-        self.work_count = torch.zeros(4, dtype=torch.int32, device=self.device)
+        # the three work lists of MPF3D_STEP_MULTI_LIST and their counters
+        self.work_items = torch.empty(2 * self.total_cells, dtype=torch.int32, device=self.device)
+        self.work_count = torch.zeros(6, dtype=torch.int32, device=self.device)
         self.buf = [self._alloc(), self._alloc()]
         self.cur = 0
         self.step_count = 0
@@ -181,7 +182,7 @@ class BatchedBicrystals:
             self.wij.data_ptr(), self.a2ij.data_ptr(), self.mij.data_ptr(), self.n111.data_ptr(), 3,
             ctypes.byref(self.scalars), int(self.anisotropy), int(self.torque), int(self.symmetric_normals),
             self.work_items.data_ptr(), self.work_count.data_ptr(), self.step_count & 1,
-            self.err.data_ptr(), self._stream())
+            self.err.data_ptr(), self._stream(), _lib.STEP_MULTI_LIST)
         _lib.check(rc, "batched_step")
         self.cur = 1 - self.cur
 
