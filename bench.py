@@ -133,6 +133,36 @@ def measured_peak():
         return FALLBACK_HBM_GBS, "fallback"
 
 
+def cell_record_bytes(solver):
+    """Bytes of every cell's record (int64 [cells], x fastest): the 4-byte
+    head plus 6 bytes per stored phase of cells holding two or more (4 for
+    an explicitly stored single value)."""
+    import torch
+    h = solver.buf[solver.cur][0]
+    n = (h & 0x7F).long()
+    e = ((h >> 7) & 1).long()
+    return 4 + torch.where(n >= 2, 6 * n - 2, 4 * e)
+
+
+def quiet_cells(solver, step_index):
+    """Cells (bool [cells], x fastest) in the tiles that the step
+    `step_index` skips: tiles that were uniform, with their 6 neighbours, in
+    the previous step (the rule of the sweep kernel)."""
+    import torch
+    zb = solver.tuning.sweep_zb if solver.tuning is not None else 4
+    nx, ny, nz = solver.nx, solver.ny, solver.nz
+    ntx, nkb = -(-nx // 32), -(-nz // zb)
+    n = nkb * ny * ntx
+    if not solver.skip_quiet_tiles or solver._tiles_zb != zb:
+        return torch.zeros(solver.cells, dtype=torch.bool, device=solver.device)
+    half = (step_index & 1) ^ 1
+    f = solver.tile_flags[half * n:(half + 1) * n].view(nkb, ny, ntx).bool()
+    q = f & torch.roll(f, 1, 2) & torch.roll(f, -1, 2) & torch.roll(f, 1, 1) & torch.roll(f, -1, 1)
+    q = q & torch.cat([f[1:], f[-1:]], 0) & torch.cat([f[:1], f[:-1]], 0)
+    q = q.repeat_interleave(zb, 0)[:nz].repeat_interleave(32, 2)[:, :, :nx]
+    return q.reshape(-1)
+
+
 def committed_traffic():
     """Per-launch DRAM bytes of the step kernel from the committed ncu summary."""
     path = os.path.join(ROOT, "profiles", "compact_step_256cube.txt")
@@ -268,22 +298,34 @@ def run_ours(args, rank, world):
         ms = float(t.item())
     final_cnt_sum = int(solver.stored_counts().sum(dtype=torch.int64).item())
 
-    # accounting pass (untimed): record bytes of the state before and after
-    # every step, and the stored-phase occupancy
+    # accounting pass (untimed), the same run again: per step, the record
+    # bytes of the cells the step visits (read of the old record, write of
+    # the new one; cells of tiles skipped as quiet move nothing), the quiet
+    # share and the stored-phase occupancy
     acc = CompactSolver(phi0, temp, n111, wij, aij, mij, phys, slots=args.slots)
     acc.tuning = tuning
     occ = [int(acc.stored_counts().sum(dtype=torch.int64).item())]
-    rec = [acc.record_bytes()]
+    rec_all = 0
+    bytes_total = 0
+    quiet_share = 0.0
+    r_prev = cell_record_bytes(acc)
     for i in range(args.steps):
+        skip = quiet_cells(acc, i + 1)
         acc.launch_step(i + 1)
+        r_next = cell_record_bytes(acc)
+        both = r_prev + r_next
+        rec_all += int(both.sum().item())
+        bytes_total += int(both[~skip].sum().item())
+        quiet_share += float(skip.float().mean().item())
         occ.append(int(acc.stored_counts().sum(dtype=torch.int64).item()))
-        rec.append(acc.record_bytes())
+        r_prev = r_next
     acc.check()
     del acc
     cells = nx * ny * nz
-    # algorithmic bytes: every cell's record read once and written once
-    bytes_total = sum(rec[i] + rec[i + 1] for i in range(args.steps))
+    # algorithmic bytes: every visited cell's record read once and written once
     bytes_per_launch = bytes_total / args.steps
+    full_state_bytes = rec_all / args.steps
+    quiet_share /= args.steps
     sec = ms / 1e3
     value = cells * args.steps * world / sec
     per_launch_s = sec / args.steps
@@ -315,7 +357,9 @@ def run_ours(args, rank, world):
     if rank == 0 and not args.no_bicrystal and args.bicrystal_steps > 0:
         extra["bicrystal_batch"] = bicrystal_run(args, dev)
     emit(args, rank, world, value, ms, cells, t_e2e, in_bytes, out_bytes, achieved, peak, peak_kind,
-         traffic, bytes_per_launch, occ, clk, cpu, final_cnt_sum, extra)
+         traffic, bytes_per_launch, occ, clk, cpu, final_cnt_sum, dict(extra, quiet_tile_share=quiet_share,
+                                                                         full_state_bytes_per_cell_step=
+                                                                         full_state_bytes / cells))
 
 
 def e2e_run(args, phi0, temp, n111, wij, aij, mij, phys, dev, barrier, world, tuning=None):
@@ -480,6 +524,8 @@ def emit(args, rank, world, value, ms, cells, t_e2e, in_bytes, out_bytes, achiev
                              "frac": achieved / peak, "traffic": traffic,
                              "peak_source": peak_kind,
                              "bytes_per_cell_step": bytes_per_launch / cells,
+                             "bytes_basis": "records of the cells in the tiles each step visits, read + "
+                                            "written once (quiet tiles move nothing)",
                              "kernel": f"sweep+general+interface kernels <{args.slots},{2 * args.slots}>",
                              "traffic_unit": "bytes per step (3 launches), from the committed ncu summary"},
                 "stored_phases_per_cell": {"start": occ[0] / cells, "end": occ[-1] / cells},
