@@ -41,6 +41,7 @@ GRID = (256, 256, 256)
 N_GRAINS = 64
 SLAB = 32
 SEED, ORIENT_SEED = 2026, 7
+FALLBACK_BF16_TFLOPS = 1900.0
 FALLBACK_HBM_GBS = 6800.0
 
 
@@ -131,6 +132,52 @@ def measured_peak():
             return float(json.load(f)["hbm_gbs"]), "measured"
     except (OSError, KeyError, ValueError):
         return FALLBACK_HBM_GBS, "fallback"
+
+
+def gemm_run(dev, M=65536, N=256, K=256, reps=20):
+    """The surrogate's hidden-layer GEMM (Y = SiLU(X W^T + b), BF16 in, FP32
+    accumulate, BF16 out) at the screening batch: the tcgen05 kernel and the
+    mma.sync kernel, timed with CUDA events, against the measured dense BF16
+    peak (burst: the kernel is timed alone)."""
+    import torch
+    from mpf3d import _lib
+    L = _lib.lib()
+    g = torch.Generator(device="cpu").manual_seed(5)
+    X = (torch.randn((M, K), generator=g) * 0.5).to(torch.bfloat16).to(dev)
+    W = (torch.randn((N, K), generator=g) * 0.06).to(torch.bfloat16).to(dev)
+    b = torch.zeros(N, dtype=torch.float32, device=dev)
+    Y = torch.empty((M, N), dtype=torch.bfloat16, device=dev)
+    st = torch.cuda.current_stream(dev)
+    calls = {
+        "tc5": lambda: L.mpf3d_gemm_bf16_tc5(M, N, K, X.data_ptr(), K, W.data_ptr(), K, b.data_ptr(), 1, None,
+                                             Y.data_ptr(), N, 1, 0, st.cuda_stream or None),
+        "mma": lambda: L.mpf3d_gemm_bf16_mma(M, N, K, X.data_ptr(), K, 1, W.data_ptr(), 1, K, b.data_ptr(), 1, None,
+                                             Y.data_ptr(), N, 1, 0, st.cuda_stream or None),
+    }
+    out = {"shape": [M, N, K], "flop": 2.0 * M * N * K}
+    for name, fn in calls.items():
+        for _ in range(3):
+            assert fn() == 0
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize(dev)
+        e0.record(st)
+        for _ in range(reps):
+            fn()
+        e1.record(st)
+        torch.cuda.synchronize(dev)
+        us = e0.elapsed_time(e1) * 1e3 / reps
+        out[f"{name}_us"] = us
+        out[f"{name}_tflops"] = out["flop"] / (us * 1e-6) / 1e12
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peak = float(json.load(f)["bf16_tflops"])
+        out["peak_bf16_tflops"], out["peak_source"] = peak, "measured (burst)"
+    except (OSError, KeyError, ValueError):
+        peak = FALLBACK_BF16_TFLOPS
+        out["peak_bf16_tflops"], out["peak_source"] = peak, "fallback"
+    out["tc5_frac"] = out["tc5_tflops"] / peak
+    out["mma_frac"] = out["mma_tflops"] / peak
+    return out
 
 
 def cell_record_bytes(solver):
@@ -356,6 +403,8 @@ def run_ours(args, rank, world):
     torch.cuda.empty_cache()
     if rank == 0 and not args.no_bicrystal and args.bicrystal_steps > 0:
         extra["bicrystal_batch"] = bicrystal_run(args, dev)
+    if rank == 0 and not args.no_gemm:
+        extra["surrogate_gemm"] = gemm_run(dev)
     emit(args, rank, world, value, ms, cells, t_e2e, in_bytes, out_bytes, achieved, peak, peak_kind,
          traffic, bytes_per_launch, occ, clk, cpu, final_cnt_sum, dict(extra, quiet_tile_share=quiet_share,
                                                                          full_state_bytes_per_cell_step=
@@ -614,6 +663,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end run (profiling)")
     ap.add_argument("--no-autotune", action="store_true", help="use the default launch shape")
+    ap.add_argument("--no-gemm", action="store_true", help="skip the surrogate GEMM measurement")
     ap.add_argument("--grid", type=int, nargs=3, default=None,
                     help="override the 256^3 grid (smaller cases for profiling)")
     ap.add_argument("--accuracy-steps", type=int, default=100)

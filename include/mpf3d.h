@@ -354,10 +354,22 @@ int mpf3d_batched_ray_radii(const uint32_t *head, const uint16_t *idx, const flo
 /* C[m][n] = act(sum_k A(m,k) B(k,n) + bias[n]) with A(m,k) = A[m*sam + k*sak],
  * B(k,n) = B[k*sbk + n*sbn]; act 0 = none, 1 = SiLU.  Z (nullable) receives
  * the FP32 pre-activation, Y the result (BF16 if y_bf16, else FP32, added to
- * Y when beta = 1), both with row stride ldy.  mma.sync m16n8k16 tiles. */
+ * Y when beta = 1), both with row stride ldy.  K-major operands that fit
+ * mpf3d_gemm_bf16_tc5 run there, the rest on mpf3d_gemm_bf16_mma. */
 int mpf3d_gemm_bf16(int M, int N, int K, const uint16_t *A, int64_t sam, int64_t sak, const uint16_t *B,
                     int64_t sbk, int64_t sbn, const float *bias, int act, float *Z, void *Y, int ldy,
                     int y_bf16, int beta, void *stream);
+
+/* The two kernels behind mpf3d_gemm_bf16, callable directly.  _tc5: the
+ * tcgen05 kernel (M x N tiles of 128 x N in tensor memory) for K-major A
+ * [M][K] (row stride lda) and B given as [N][K] (row stride ldb), K a
+ * multiple of 16 up to 256, N up to 256, 16-byte aligned rows; other shapes
+ * return MPF3D_ERR_ARG.  _mma: the mma.sync kernel, any strides. */
+int mpf3d_gemm_bf16_tc5(int M, int N, int K, const uint16_t *A, int64_t lda, const uint16_t *B, int64_t ldb,
+                        const float *bias, int act, float *Z, void *Y, int ldy, int y_bf16, int beta, void *stream);
+int mpf3d_gemm_bf16_mma(int M, int N, int K, const uint16_t *A, int64_t sam, int64_t sak, const uint16_t *B,
+                        int64_t sbk, int64_t sbn, const float *bias, int act, float *Z, void *Y, int ldy,
+                        int y_bf16, int beta, void *stream);
 
 /* dZ = dY * act'(Z) elementwise; outputs BF16 and/or FP32 (each nullable). */
 int mpf3d_act_backward(const float *dY, const float *Z, int act, int64_t n, uint16_t *dZ16, float *dZ32,

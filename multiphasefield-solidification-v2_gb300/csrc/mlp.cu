@@ -9,8 +9,11 @@
 // arbitrary operand strides serves the forward pass (X W^T), the input
 // gradient (dZ W) and the weight gradient (dZ^T X) alike.
 //
-// The GEMM uses mma.sync.m16n8k16 (BF16 in, FP32 accumulate) from shared
-// memory tiles: 64 x 64 output tile per CTA, 4 warps of 32 x 32, k step 32.
+// Two GEMM kernels: K-major operands (the forward pass X W^T, K <= 256,
+// N <= 256) run on the fifth-generation tensor cores (tcgen05.mma with the
+// accumulator in tensor memory); transposed operands (the gradients) use
+// mma.sync.m16n8k16 (BF16 in, FP32 accumulate) from shared memory tiles:
+// 64 x 64 output tile per CTA, 4 warps of 32 x 32, k step 32.
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdint.h>
@@ -206,15 +209,302 @@ int grid_for(int64_t n) {
 }
 }  // namespace
 
-extern "C" int mpf3d_gemm_bf16(int M, int N, int K, const uint16_t *A, int64_t sam, int64_t sak, const uint16_t *B,
-                               int64_t sbk, int64_t sbn, const float *bias, int act, float *Z, void *Y, int ldy,
-                               int y_bf16, int beta, void *stream) {
+// ---------------------------------------------------------------------------
+// The K-major GEMM on the fifth-generation tensor cores (tcgen05).  One CTA
+// of 128 threads computes a 128 x N tile (N <= 256) with K <= 256:
+//   1. the threads stage A [128][K] and B [N][K] (BF16, K contiguous in
+//      global memory) in shared memory in the canonical K-major layout
+//      without swizzle: 8-row x 16-byte core matrices, the cores of one
+//      8-row block adjacent along K (leading byte offset 128), row blocks
+//      K/8 cores apart (stride byte offset);
+//   2. warp 0 allocates N columns of tensor memory for the FP32
+//      accumulator; one thread issues K/16 tcgen05.mma (M = 128, N, K = 16,
+//      kind::f16 with BF16 inputs) and commits them to an mbarrier;
+//   3. every warp reads its 32 accumulator rows back with tcgen05.ld
+//      (32x32b shape, 16 columns at a time) and applies bias, SiLU and the
+//      stores of the mma.sync kernel's epilogue, as 16-byte vectors.
+// The CTAs are persistent (one or two per SM): B is staged once per CTA,
+// the tensor memory allocated once, and the mbarrier phase alternates with
+// the tiles.
+// The mbarrier poll is bounded: a step that never completes writes NaN
+// instead of results, waits once more and still frees its tensor memory.
+namespace mpf3d {
+namespace mlp {
+namespace tc5 {
+
+constexpr int TM = 128;
+constexpr int MAX_N = 256;
+constexpr int MAX_K = 256;
+constexpr uint32_t POLL_LIMIT = 1u << 24;
+
+__device__ __forceinline__ uint32_t smem_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// shared-memory matrix descriptor: start address, leading and stride byte
+// offsets (all >> 4), descriptor version 1, no swizzle
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+    return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+           ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | ((uint64_t)1 << 46);
+}
+
+// instruction descriptor of kind::f16: FP32 accumulator, BF16 A and B,
+// both K-major, N >> 3 and M >> 4
+__host__ __device__ __forceinline__ uint32_t instr_desc(int m, int n) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
+}
+
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+    for (uint32_t it = 0; it < POLL_LIMIT; ++it) {
+        uint32_t ok;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.b32 %0, 1, 0, p;\n}\n"
+            : "=r"(ok)
+            : "r"(bar), "r"(parity)
+            : "memory");
+        if (ok) return true;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+}
+
+__device__ __forceinline__ void stage(uint8_t *dst, const uint16_t *__restrict__ src, int64_t ld, int rows_valid,
+                                      int rows, int K) {
+    // chunk e is row (e % 8) of core (e / 8): 8 consecutive threads fill one
+    // 128-byte core matrix; 8 chunks per thread are loaded before any is
+    // stored, so the loads overlap
+    const int kc = K / 8;
+    const uint32_t sbo = (uint32_t)kc * 128u;
+    const int total = rows * kc;
+    constexpr int U = 8;
+    for (int e0 = threadIdx.x; e0 < total; e0 += U * blockDim.x) {
+        uint4 v[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int e = e0 + u * blockDim.x;
+            v[u] = make_uint4(0u, 0u, 0u, 0u);
+            if (e < total) {
+                const int core = e >> 3, r8 = e & 7;
+                const int rb = core / kc, c = core - rb * kc;
+                const int r = rb * 8 + r8;
+                if (r < rows_valid) v[u] = __ldg(reinterpret_cast<const uint4 *>(src + (int64_t)r * ld + c * 8));
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int e = e0 + u * blockDim.x;
+            if (e < total) {
+                const int core = e >> 3, r8 = e & 7;
+                const int rb = core / kc, c = core - rb * kc;
+                *reinterpret_cast<uint4 *>(dst + rb * sbo + c * 128u + r8 * 16u) = v[u];
+            }
+        }
+    }
+}
+
+// Persistent CTAs: each stages B once, then loops over 128-row tiles of A.
+__global__ void __launch_bounds__(128) gemm_kernel(int M, int N, int K, const uint16_t *__restrict__ A, int64_t lda,
+                                                   const uint16_t *__restrict__ B, int64_t ldb,
+                                                   const float *__restrict__ bias, int act, float *__restrict__ Z,
+                                                   void *__restrict__ Y, int ldy, int y_bf16, int beta) {
+    extern __shared__ __align__(1024) uint8_t smem[];
+    const int n_mma = (N + 15) & ~15;
+    uint8_t *sA = smem;
+    uint8_t *sB = smem + TM * K * 2;
+    uint64_t *bar = reinterpret_cast<uint64_t *>(sB + n_mma * K * 2);
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(bar + 1);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t ncols = n_mma <= 32 ? 32u : (n_mma <= 64 ? 64u : (n_mma <= 128 ? 128u : 256u));
+    const int tiles = (M + TM - 1) / TM;
+
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_addr(bar)) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_addr(tslot)),
+                     "r"(ncols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+    }
+    stage(sB, B, ldb, N, n_mma, K);
+    const uint32_t bar_a = smem_addr(bar);
+    const uint32_t idesc = instr_desc(TM, n_mma);
+    const uint32_t a0 = smem_addr(sA), b0 = smem_addr(sB), sbo = (uint32_t)(K / 8) * 128u;
+    const bool vec_ok = (ldy % 8 == 0) && (((uintptr_t)Y & 15u) == 0) && (!Z || ((uintptr_t)Z & 15u) == 0);
+    uint32_t tmem = 0;
+    bool ok = true;
+    int it = 0;
+    for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x, ++it) {
+        const int m0 = tile * TM;
+        stage(sA, A + (int64_t)m0 * lda, lda, min(TM, M - m0), TM, K);
+        // the tensor core reads shared memory through the async proxy; the
+        // previous tile's accumulator reads are complete (barrier below)
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+        __syncthreads();
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+        tmem = *tslot;
+        if (threadIdx.x == 0) {
+            for (int ks = 0; ks < K / 16; ++ks) {
+                const uint64_t ad = smem_desc(a0 + ks * 256u, 128u, sbo);
+                const uint64_t bd = smem_desc(b0 + ks * 256u, 128u, sbo);
+                const uint32_t accum = ks > 0 ? 1u : 0u;
+                asm volatile(
+                    "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                    " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+                    "l"(ad), "l"(bd), "r"(idesc), "r"(accum)
+                    : "memory");
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(bar_a)
+                         : "memory");
+        }
+        // tcgen05.ld is warp-collective: a warp reads the accumulator only
+        // if all of its lanes saw the commit; a missed commit ends the loop
+        // for the whole CTA
+        const bool done = __syncthreads_and(mbar_wait(bar_a, (uint32_t)(it & 1))) != 0;
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+        const int m = m0 + warp * 32 + lane;
+        for (int c0 = 0; c0 < n_mma; c0 += 16) {
+            uint32_t r[16];
+            if (done) tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, r);
+            if (m >= M) continue;
+            float z[16], y[16];
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+                const int n = c0 + j;
+                const float acc = done ? __uint_as_float(r[j]) : __int_as_float(0x7fc00000);
+                z[j] = acc + ((bias && n < N) ? bias[n] : 0.0f);
+                y[j] = act == 1 ? silu(z[j]) : z[j];
+            }
+            const int64_t o = (int64_t)m * ldy + c0;
+            if (vec_ok && c0 + 16 <= N) {
+                // 16 consecutive columns of one row: whole 16-byte vectors
+                if (Z) {
+#pragma unroll
+                    for (int q = 0; q < 4; ++q)
+                        reinterpret_cast<float4 *>(Z + o)[q] =
+                            make_float4(z[4 * q], z[4 * q + 1], z[4 * q + 2], z[4 * q + 3]);
+                }
+                if (y_bf16) {
+                    uint32_t w[8];
+#pragma unroll
+                    for (int q = 0; q < 8; ++q)
+                        w[q] = (uint32_t)f32_to_bf16(y[2 * q]) | ((uint32_t)f32_to_bf16(y[2 * q + 1]) << 16);
+                    uint4 *yp = reinterpret_cast<uint4 *>(static_cast<uint16_t *>(Y) + o);
+                    yp[0] = make_uint4(w[0], w[1], w[2], w[3]);
+                    yp[1] = make_uint4(w[4], w[5], w[6], w[7]);
+                } else {
+                    float4 *yp = reinterpret_cast<float4 *>(static_cast<float *>(Y) + o);
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        float4 v = make_float4(y[4 * q], y[4 * q + 1], y[4 * q + 2], y[4 * q + 3]);
+                        if (beta) {
+                            const float4 prev = yp[q];
+                            v.x += prev.x; v.y += prev.y; v.z += prev.z; v.w += prev.w;
+                        }
+                        yp[q] = v;
+                    }
+                }
+            } else {
+#pragma unroll
+                for (int j = 0; j < 16; ++j) {
+                    const int n = c0 + j;
+                    if (n >= N) break;
+                    if (Z) Z[o + j] = z[j];
+                    if (y_bf16) {
+                        static_cast<uint16_t *>(Y)[o + j] = f32_to_bf16(y[j]);
+                    } else {
+                        float *yf = static_cast<float *>(Y);
+                        yf[o + j] = beta ? yf[o + j] + y[j] : y[j];
+                    }
+                }
+            }
+        }
+        asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+        __syncthreads();
+        if (!done) {
+            ok = false;
+            break;
+        }
+    }
+    if (!ok) mbar_wait(bar_a, (uint32_t)(it & 1));  // let an overdue MMA drain before the memory is freed
+    __syncthreads();
+    if (warp == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+        tmem = *tslot;
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(ncols) : "memory");
+    }
+}
+
+inline size_t smem_bytes(int N, int K) {
+    const int n_mma = (N + 15) & ~15;
+    const size_t need = (size_t)(TM + n_mma) * K * 2 + 16;
+    // at least 80 KB keeps two CTAs per SM at most: 2 x 256 tensor-memory
+    // columns fit the SM's 512, so an allocation never waits for another CTA
+    return need < 80 * 1024 ? 80 * 1024 : need;
+}
+
+}  // namespace tc5
+}  // namespace mlp
+}  // namespace mpf3d
+
+static int sms_of_device() {
+    int dev = 0, sms = 148;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    return sms;
+}
+
+static bool tc5_shape_ok(int M, int N, int K, const uint16_t *A, int64_t lda, const uint16_t *B, int64_t ldb) {
+    return M > 0 && N > 0 && N <= mpf3d::mlp::tc5::MAX_N && K >= 16 && K <= mpf3d::mlp::tc5::MAX_K && K % 16 == 0 &&
+           lda >= K && ldb >= K && lda % 8 == 0 && ldb % 8 == 0 && ((uintptr_t)A & 15u) == 0 &&
+           ((uintptr_t)B & 15u) == 0;
+}
+
+extern "C" int mpf3d_gemm_bf16_tc5(int M, int N, int K, const uint16_t *A, int64_t lda, const uint16_t *B,
+                                   int64_t ldb, const float *bias, int act, float *Z, void *Y, int ldy, int y_bf16,
+                                   int beta, void *stream) {
+    using namespace mpf3d::mlp;
+    if (!A || !B || !Y || ldy < N || (act != 0 && act != 1) || !tc5_shape_ok(M, N, K, A, lda, B, ldb))
+        return MPF3D_ERR_ARG;
+    const size_t bytes = tc5::smem_bytes(N, K);
+    if (cudaFuncSetAttribute(tc5::gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) !=
+        cudaSuccess)
+        return MPF3D_ERR_CUDA;
+    const int tiles = (M + tc5::TM - 1) / tc5::TM;
+    const int per_sm = bytes > 114 * 1024 ? 1 : 2;
+    const int grid = tiles < sms_of_device() * per_sm ? tiles : sms_of_device() * per_sm;
+    tc5::gemm_kernel<<<grid, 128, bytes, (cudaStream_t)stream>>>(M, N, K, A, lda, B, ldb, bias, act, Z, Y, ldy,
+                                                                 y_bf16, beta);
+    return cudaGetLastError() == cudaSuccess ? MPF3D_OK : MPF3D_ERR_CUDA;
+}
+
+extern "C" int mpf3d_gemm_bf16_mma(int M, int N, int K, const uint16_t *A, int64_t sam, int64_t sak,
+                                   const uint16_t *B, int64_t sbk, int64_t sbn, const float *bias, int act, float *Z,
+                                   void *Y, int ldy, int y_bf16, int beta, void *stream) {
     if (M <= 0 || N <= 0 || K <= 0 || !A || !B || !Y || ldy < N || (act != 0 && act != 1)) return MPF3D_ERR_ARG;
     if ((M + BM - 1) / BM > 65535) return MPF3D_ERR_TOO_LARGE;
     dim3 grid((N + BN - 1) / BN, (M + BM - 1) / BM);
     gemm_bf16_kernel<<<grid, 128, 0, (cudaStream_t)stream>>>(M, N, K, A, sam, sak, B, sbk, sbn, bias, act, Z, Y, ldy,
                                                              y_bf16, beta);
     return cudaGetLastError() == cudaSuccess ? MPF3D_OK : MPF3D_ERR_CUDA;
+}
+
+extern "C" int mpf3d_gemm_bf16(int M, int N, int K, const uint16_t *A, int64_t sam, int64_t sak, const uint16_t *B,
+                               int64_t sbk, int64_t sbn, const float *bias, int act, float *Z, void *Y, int ldy,
+                               int y_bf16, int beta, void *stream) {
+    // K-major operands (the forward pass X W^T) go to the tcgen05 kernel;
+    // transposed ones (the gradients) to the mma.sync kernel
+    if (sak == 1 && sbk == 1 && tc5_shape_ok(M, N, K, A, sam, B, sbn))
+        return mpf3d_gemm_bf16_tc5(M, N, K, A, sam, B, sbn, bias, act, Z, Y, ldy, y_bf16, beta, stream);
+    return mpf3d_gemm_bf16_mma(M, N, K, A, sam, sak, B, sbk, sbn, bias, act, Z, Y, ldy, y_bf16, beta, stream);
 }
 
 extern "C" int mpf3d_act_backward(const float *dY, const float *Z, int act, int64_t n, uint16_t *dZ16, float *dZ32,

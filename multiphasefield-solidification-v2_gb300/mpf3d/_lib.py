@@ -87,6 +87,10 @@ _SIGS = {
     "mpf3d_compact_init_owner": (_I32, [_VP, _I32, _VP, _I32, _I32, _I32, _I32, _VP, _VP, _VP, _VP]),
     "mpf3d_gemm_bf16": (_I32, [_I32, _I32, _I32, _VP, _I64, _I64, _VP, _I64, _I64, _VP, _I32, _VP, _VP, _I32,
                                _I32, _I32, _VP]),
+    "mpf3d_gemm_bf16_mma": (_I32, [_I32, _I32, _I32, _VP, _I64, _I64, _VP, _I64, _I64, _VP, _I32, _VP, _VP, _I32,
+                               _I32, _I32, _VP]),
+    "mpf3d_gemm_bf16_tc5": (_I32, [_I32, _I32, _I32, _VP, _I64, _VP, _I64, _VP, _I32, _VP, _VP, _I32, _I32, _I32,
+                                   _VP]),
     "mpf3d_act_backward": (_I32, [_VP, _VP, _I32, _I64, _VP, _VP, _VP]),
     "mpf3d_colsum": (_I32, [_VP, _I32, _I32, _I32, _VP, _VP]),
     "mpf3d_mse": (_I32, [_VP, _I32, _VP, _I32, _I32, _VP, _VP, _VP, _VP]),

@@ -51,6 +51,54 @@ def test_gemm_matches_float64(M, N, K, transA, transB):
     assert np.abs(got_y - ref_y).max() <= 1e-3 * scale
 
 
+@pytest.mark.parametrize("M,N,K,act,y_bf16", [(300, 256, 256, 1, 1), (128, 256, 16, 1, 0), (77, 16, 256, 0, 0),
+                                             (1000, 128, 64, 1, 1), (129, 2, 256, 0, 0), (256, 200, 32, 0, 0)])
+def test_tcgen05_gemm_matches_float64(M, N, K, act, y_bf16):
+    """The tensor-memory kernel (K-major X [M][K], W [N][K]) against a float64
+    product of the same BF16 operands, and against the mma.sync kernel."""
+    from mpf3d import _lib
+    rng = np.random.default_rng(M * 7 + N + K)
+    X = rng.standard_normal((M, K)).astype(np.float32)
+    W = rng.standard_normal((N, K)).astype(np.float32)
+    bias = rng.standard_normal(N).astype(np.float32)
+    dev = torch.device("cuda:0")
+    tX = torch.from_numpy(to_bf16_bits(X)).to(dev)
+    tW = torch.from_numpy(to_bf16_bits(W)).to(dev)
+    tb = torch.from_numpy(bias).to(dev)
+    ydt = torch.int16 if y_bf16 else torch.float32
+    Z = torch.full((M, N), float("nan"), dtype=torch.float32, device=dev)
+    Y = torch.zeros((M, N), dtype=ydt, device=dev)
+    rc = _lib.lib().mpf3d_gemm_bf16_tc5(M, N, K, tX.data_ptr(), K, tW.data_ptr(), K, tb.data_ptr(), act,
+                                        Z.data_ptr(), Y.data_ptr(), N, y_bf16, 0, None)
+    assert rc == 0
+    ref_z = bf16_round(X) @ bf16_round(W).T + bias
+    got_z = Z.cpu().numpy()
+    scale = np.abs(ref_z).max()
+    assert np.isfinite(got_z).all()
+    assert np.abs(got_z - ref_z).max() <= 1e-5 * scale * np.sqrt(K)
+    Z2 = torch.empty((M, N), dtype=torch.float32, device=dev)
+    Y2 = torch.zeros((M, N), dtype=ydt, device=dev)
+    rc = _lib.lib().mpf3d_gemm_bf16_mma(M, N, K, tX.data_ptr(), K, 1, tW.data_ptr(), 1, K, tb.data_ptr(), act,
+                                        Z2.data_ptr(), Y2.data_ptr(), N, y_bf16, 0, None)
+    assert rc == 0
+    assert np.abs(Z2.cpu().numpy() - got_z).max() <= 1e-5 * scale * np.sqrt(K)
+    if y_bf16:
+        ya = (Y.cpu().numpy().view(np.uint16).astype(np.uint32) << 16).view(np.float32)
+        yb = (Y2.cpu().numpy().view(np.uint16).astype(np.uint32) << 16).view(np.float32)
+        assert np.abs(ya - yb).max() <= 1e-2 * max(1.0, np.abs(yb).max())
+    else:
+        assert np.abs(Y.cpu().numpy() - Y2.cpu().numpy()).max() <= 1e-4 * scale * np.sqrt(K)
+
+
+def test_tcgen05_rejects_shapes_it_does_not_cover():
+    from mpf3d import _lib
+    L = _lib.lib()
+    p = 0x10000
+    assert L.mpf3d_gemm_bf16_tc5(64, 300, 64, p, 64, p, 64, None, 0, None, p, 300, 0, 0, None) == -1  # N > 256
+    assert L.mpf3d_gemm_bf16_tc5(64, 64, 24, p, 24, p, 24, None, 0, None, p, 64, 0, 0, None) == -1    # K % 16
+    assert L.mpf3d_gemm_bf16_tc5(64, 64, 512, p, 512, p, 512, None, 0, None, p, 64, 0, 0, None) == -1  # K > 256
+
+
 def cpu_forward_backward(layers, X, target, w):
     """Float64 restatement of Surrogate.forward/backward with the GPU's BF16
     rounding points: hidden activations and the dZ operands of the GEMMs are
