@@ -14,9 +14,13 @@
 // accumulator in tensor memory); transposed operands (the gradients) use
 // mma.sync.m16n8k16 (BF16 in, FP32 accumulate) from shared memory tiles:
 // 64 x 64 output tile per CTA, 4 warps of 32 x 32, k step 32.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdint.h>
+
+#include <mutex>
 
 #include "mpf3d.h"
 #include "mpf3d_internal.h"
@@ -443,6 +447,271 @@ __global__ void __launch_bounds__(128) gemm_kernel(int M, int N, int K, const ui
     }
 }
 
+// ---------------------------------------------------------------------------
+// The pipelined form for K a multiple of 64: warp-specialised persistent CTAs
+// of 192 threads.
+//   warp 0 (one lane)  TMA producer: the weights once (K/64 boxes of
+//                      64 x N, 128-byte swizzle), then per tile K/64 boxes of
+//                      64 x 128 of X into a 4-stage ring (full/empty
+//                      mbarriers, transaction-counted);
+//   warp 1 (one lane)  MMA issuer: per ring stage 4 tcgen05.mma (K = 16 each,
+//                      start address +32 bytes inside the swizzled 128-byte
+//                      rows), a commit frees the stage; per tile a commit
+//                      hands the accumulator to the epilogue;
+//   warps 2-5          epilogue: tcgen05.ld of their 32-lane quarter of the
+//                      accumulator, bias, SiLU, 16-byte stores, then release
+//                      the accumulator buffer.
+// Two accumulator buffers in tensor memory let the epilogue of one tile run
+// under the MMAs of the next.  Every mbarrier wait is bounded; a wait that
+// runs out raises a CTA-wide abort flag, every role leaves its loop, the
+// producer waits for the copies it issued and the tensor memory is freed.
+namespace tma {
+
+constexpr int STAGES = 4;
+constexpr int ATOM_K = 64;                    // bf16 elements per 128-byte swizzled row
+constexpr int A_STAGE_BYTES = TM * ATOM_K * 2;  // 16 KB
+
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t addr) {
+    // K-major, 128-byte swizzle: 8-row groups 1024 bytes apart (stride byte
+    // offset); the leading byte offset is unused by this layout
+    return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) |
+           ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
+}
+
+__device__ __forceinline__ void arrive_expect(uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void arrive(uint32_t bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ void tma_load(uint32_t dst, const CUtensorMap *map, int x, int y, uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];\n" ::"r"(
+            dst),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar)
+        : "memory");
+}
+
+__device__ __forceinline__ void umma(uint32_t tmem, uint64_t ad, uint64_t bd, uint32_t idesc, uint32_t accum) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+        "l"(ad), "l"(bd), "r"(idesc), "r"(accum)
+        : "memory");
+}
+
+__device__ __forceinline__ void commit(uint32_t bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(bar)
+                 : "memory");
+}
+
+__global__ void __launch_bounds__(192, 1) gemm_kernel(const __grid_constant__ CUtensorMap map_x,
+                                                      const __grid_constant__ CUtensorMap map_w, int M, int N, int K,
+                                                      const float *__restrict__ bias, int act,
+                                                      float *__restrict__ Z, void *__restrict__ Y, int ldy,
+                                                      int y_bf16, int beta) {
+    extern __shared__ __align__(1024) uint8_t smem_raw[];
+    // 1024-byte alignment for the swizzled tiles
+    uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
+    const int n_mma = (N + 15) & ~15;
+    const int KA = K / ATOM_K;
+    const uint32_t w_atom_bytes = (uint32_t)n_mma * 128u;
+    uint8_t *sW = smem;
+    uint8_t *sA = sW + KA * w_atom_bytes;
+    uint64_t *bars = reinterpret_cast<uint64_t *>(sA + STAGES * A_STAGE_BYTES);
+    // bars: full[STAGES], empty[STAGES], acc_full[2], acc_empty[2], w_full
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(bars + 2 * STAGES + 5);
+    int *abort_flag = reinterpret_cast<int *>(tslot + 1);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t buf_cols = n_mma <= 32 ? 32u : (n_mma <= 64 ? 64u : (n_mma <= 128 ? 128u : 256u));
+    const int tiles = (M + TM - 1) / TM;
+    auto bar = [&](int i) { return smem_addr(bars + i); };
+    const int FULL = 0, EMPTY = STAGES, ACC_FULL = 2 * STAGES, ACC_EMPTY = 2 * STAGES + 2, W_FULL = 2 * STAGES + 4;
+
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < STAGES; ++i) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar(FULL + i)) : "memory");
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar(EMPTY + i)) : "memory");
+        }
+        for (int b = 0; b < 2; ++b) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar(ACC_FULL + b)) : "memory");
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 4;\n" ::"r"(bar(ACC_EMPTY + b)) : "memory");
+        }
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar(W_FULL)) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+        *abort_flag = 0;
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_addr(tslot)),
+                     "r"(2 * buf_cols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    const uint32_t tmem = *tslot;
+    volatile int *abort_v = abort_flag;
+    auto wait = [&](int i, uint32_t parity) -> bool {
+        if (*abort_v) return false;
+        if (mbar_wait(bar(i), parity)) return true;
+        *abort_v = 1;
+        return false;
+    };
+
+    if (warp == 0) {
+        if (lane == 0) {
+            // weights once
+            arrive_expect(bar(W_FULL), (uint32_t)KA * w_atom_bytes);
+            for (int j = 0; j < KA; ++j) tma_load(smem_addr(sW + j * w_atom_bytes), &map_w, j * ATOM_K, 0, bar(W_FULL));
+            uint32_t it = 0, issued = 0;
+            for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+                for (int j = 0; j < KA; ++j, ++it) {
+                    const int s = it % STAGES;
+                    if (!wait(EMPTY + s, ((it / STAGES) & 1u) ^ 1u)) break;
+                    arrive_expect(bar(FULL + s), A_STAGE_BYTES);
+                    tma_load(smem_addr(sA + s * A_STAGE_BYTES), &map_x, j * ATOM_K, tile * TM, bar(FULL + s));
+                    issued = it + 1;
+                }
+                if (*abort_v) break;
+            }
+            // every copy issued must land before the CTA can go away
+            if (*abort_v) {
+                for (uint32_t q = issued > STAGES ? issued - STAGES : 0; q < issued; ++q)
+                    mbar_wait(bar(FULL + q % STAGES), (q / STAGES) & 1u);
+                mbar_wait(bar(W_FULL), 0);
+            }
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            const uint32_t idesc = instr_desc(TM, n_mma);
+            if (wait(W_FULL, 0)) {
+                uint32_t it = 0, t_local = 0;
+                for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x, ++t_local) {
+                    const uint32_t b = t_local & 1u;
+                    if (!wait(ACC_EMPTY + b, ((t_local >> 1) & 1u) ^ 1u)) break;
+                    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+                    const uint32_t d = tmem + b * buf_cols;
+                    bool ok = true;
+                    for (int j = 0; j < KA; ++j, ++it) {
+                        const int s = it % STAGES;
+                        if (!wait(FULL + s, (it / STAGES) & 1u)) {
+                            ok = false;
+                            break;
+                        }
+                        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+                        const uint32_t a_base = smem_addr(sA + s * A_STAGE_BYTES);
+                        const uint32_t w_base = smem_addr(sW + j * w_atom_bytes);
+#pragma unroll
+                        for (int ks = 0; ks < ATOM_K / 16; ++ks)
+                            umma(d, sw128_desc(a_base + 32u * ks), sw128_desc(w_base + 32u * ks), idesc,
+                                 (j > 0 || ks > 0) ? 1u : 0u);
+                        commit(bar(EMPTY + s));  // the stage is free once these MMAs are done
+                    }
+                    if (!ok) break;
+                    commit(bar(ACC_FULL + b));
+                }
+            }
+        }
+    } else {
+        // epilogue warps 2..5: warp w reads lanes 32 * (w % 4) .. + 31
+        const int q = warp & 3;
+        const bool vec_ok = (ldy % 8 == 0) && (((uintptr_t)Y & 15u) == 0) && (!Z || ((uintptr_t)Z & 15u) == 0);
+        uint32_t t_local = 0;
+        for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x, ++t_local) {
+            const uint32_t b = t_local & 1u;
+            const bool done = __all_sync(0xffffffffu, wait(ACC_FULL + b, (t_local >> 1) & 1u));
+            if (!done) break;
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+            const int m = tile * TM + q * 32 + lane;
+            for (int c0 = 0; c0 < n_mma; c0 += 16) {
+                uint32_t r[16];
+                tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + b * buf_cols + (uint32_t)c0, r);
+                if (m >= M) continue;
+                float z[16], y[16];
+#pragma unroll
+                for (int j = 0; j < 16; ++j) {
+                    const int n = c0 + j;
+                    z[j] = __uint_as_float(r[j]) + ((bias && n < N) ? bias[n] : 0.0f);
+                    y[j] = act == 1 ? silu(z[j]) : z[j];
+                }
+                const int64_t o = (int64_t)m * ldy + c0;
+                if (vec_ok && c0 + 16 <= N) {
+                    if (Z) {
+#pragma unroll
+                        for (int v = 0; v < 4; ++v)
+                            reinterpret_cast<float4 *>(Z + o)[v] =
+                                make_float4(z[4 * v], z[4 * v + 1], z[4 * v + 2], z[4 * v + 3]);
+                    }
+                    if (y_bf16) {
+                        uint32_t w[8];
+#pragma unroll
+                        for (int v = 0; v < 8; ++v)
+                            w[v] = (uint32_t)f32_to_bf16(y[2 * v]) | ((uint32_t)f32_to_bf16(y[2 * v + 1]) << 16);
+                        uint4 *yp = reinterpret_cast<uint4 *>(static_cast<uint16_t *>(Y) + o);
+                        yp[0] = make_uint4(w[0], w[1], w[2], w[3]);
+                        yp[1] = make_uint4(w[4], w[5], w[6], w[7]);
+                    } else {
+                        float4 *yp = reinterpret_cast<float4 *>(static_cast<float *>(Y) + o);
+#pragma unroll
+                        for (int v = 0; v < 4; ++v) {
+                            float4 val = make_float4(y[4 * v], y[4 * v + 1], y[4 * v + 2], y[4 * v + 3]);
+                            if (beta) {
+                                const float4 prev = yp[v];
+                                val.x += prev.x; val.y += prev.y; val.z += prev.z; val.w += prev.w;
+                            }
+                            yp[v] = val;
+                        }
+                    }
+                } else {
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) {
+                        const int n = c0 + j;
+                        if (n >= N) break;
+                        if (Z) Z[o + j] = z[j];
+                        if (y_bf16) {
+                            static_cast<uint16_t *>(Y)[o + j] = f32_to_bf16(y[j]);
+                        } else {
+                            float *yf = static_cast<float *>(Y);
+                            yf[o + j] = beta ? yf[o + j] + y[j] : y[j];
+                        }
+                    }
+                }
+            }
+            asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+            __syncwarp();
+            if (lane == 0) arrive(bar(ACC_EMPTY + b));
+        }
+    }
+    __syncwarp();  // the single-lane roles rejoin their warps before the block barrier
+    __syncthreads();
+    if (*abort_v && threadIdx.x == 0) {
+        // an aborted run: the outputs of this CTA's tiles are unreliable
+        for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x)
+            for (int r = 0; r < TM && tile * TM + r < M; ++r) {
+                const int64_t o = (int64_t)(tile * TM + r) * ldy;
+                for (int n = 0; n < N; ++n) {
+                    if (y_bf16) static_cast<uint16_t *>(Y)[o + n] = 0x7fc0;
+                    else static_cast<float *>(Y)[o + n] = __int_as_float(0x7fc00000);
+                }
+            }
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(2 * buf_cols)
+                     : "memory");
+    }
+}
+
+inline size_t smem_bytes(int N, int K) {
+    const int n_mma = (N + 15) & ~15;
+    return 1024 + (size_t)(K / ATOM_K) * n_mma * 128 + (size_t)STAGES * A_STAGE_BYTES + 256;
+}
+
+}  // namespace tma
+
 inline size_t smem_bytes(int N, int K) {
     const int n_mma = (N + 15) & ~15;
     const size_t need = (size_t)(TM + n_mma) * K * 2 + 16;
@@ -468,12 +737,58 @@ static bool tc5_shape_ok(int M, int N, int K, const uint16_t *A, int64_t lda, co
            ((uintptr_t)B & 15u) == 0;
 }
 
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link
+// dependency on libcuda)
+static PFN_cuTensorMapEncodeTiled_v12000 encode_tiled() {
+    static std::once_flag once;
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    std::call_once(once, [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    });
+    return fn;
+}
+
+// 2-D map of a row-major BF16 matrix [rows][K] (row pitch ld elements):
+// boxes of 64 x box_rows, 128-byte swizzle, rows past the end read as zero
+static bool make_map(CUtensorMap *map, const uint16_t *base, int rows, int K, int64_t ld, int box_rows) {
+    PFN_cuTensorMapEncodeTiled_v12000 fn = encode_tiled();
+    if (!fn) return false;
+    cuuint64_t dims[2] = {(cuuint64_t)K, (cuuint64_t)rows};
+    cuuint64_t strides[1] = {(cuuint64_t)ld * 2};
+    cuuint32_t box[2] = {64u, (cuuint32_t)box_rows};
+    cuuint32_t estr[2] = {1u, 1u};
+    return fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<uint16_t *>(base), dims, strides, box, estr,
+              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 extern "C" int mpf3d_gemm_bf16_tc5(int M, int N, int K, const uint16_t *A, int64_t lda, const uint16_t *B,
                                    int64_t ldb, const float *bias, int act, float *Z, void *Y, int ldy, int y_bf16,
                                    int beta, void *stream) {
     using namespace mpf3d::mlp;
     if (!A || !B || !Y || ldy < N || (act != 0 && act != 1) || !tc5_shape_ok(M, N, K, A, lda, B, ldb))
         return MPF3D_ERR_ARG;
+    if (K % tc5::tma::ATOM_K == 0) {
+        // the pipelined kernel: operands arrive by TMA
+        CUtensorMap mx, mw;
+        const int n_mma = (N + 15) & ~15;
+        if (make_map(&mx, A, M, K, lda, tc5::TM) && make_map(&mw, B, N, K, ldb, n_mma)) {
+            const size_t bytes = tc5::tma::smem_bytes(N, K);
+            if (cudaFuncSetAttribute(tc5::tma::gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) !=
+                cudaSuccess)
+                return MPF3D_ERR_CUDA;
+            const int tiles = (M + tc5::TM - 1) / tc5::TM;
+            const int grid = tiles < sms_of_device() ? tiles : sms_of_device();
+            tc5::tma::gemm_kernel<<<grid, 192, bytes, (cudaStream_t)stream>>>(mx, mw, M, N, K, bias, act, Z, Y, ldy,
+                                                                             y_bf16, beta);
+            return cudaGetLastError() == cudaSuccess ? MPF3D_OK : MPF3D_ERR_CUDA;
+        }
+    }
     const size_t bytes = tc5::smem_bytes(N, K);
     if (cudaFuncSetAttribute(tc5::gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) !=
         cudaSuccess)

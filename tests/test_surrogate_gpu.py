@@ -52,10 +52,13 @@ def test_gemm_matches_float64(M, N, K, transA, transB):
 
 
 @pytest.mark.parametrize("M,N,K,act,y_bf16", [(300, 256, 256, 1, 1), (128, 256, 16, 1, 0), (77, 16, 256, 0, 0),
-                                             (1000, 128, 64, 1, 1), (129, 2, 256, 0, 0), (256, 200, 32, 0, 0)])
+                                             (1000, 128, 64, 1, 1), (129, 2, 256, 0, 0), (256, 200, 32, 0, 0),
+                                             (513, 96, 192, 1, 0), (40000, 256, 128, 1, 1)])
 def test_tcgen05_gemm_matches_float64(M, N, K, act, y_bf16):
-    """The tensor-memory kernel (K-major X [M][K], W [N][K]) against a float64
-    product of the same BF16 operands, and against the mma.sync kernel."""
+    """The tensor-memory kernels (K-major X [M][K], W [N][K]; TMA-fed and
+    pipelined for K a multiple of 64, staged through registers otherwise)
+    against a float64 product of the same BF16 operands, and against the
+    mma.sync kernel."""
     from mpf3d import _lib
     rng = np.random.default_rng(M * 7 + N + K)
     X = rng.standard_normal((M, K)).astype(np.float32)
