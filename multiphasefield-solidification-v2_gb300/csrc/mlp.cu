@@ -40,7 +40,7 @@ __device__ __forceinline__ uint16_t f32_to_bf16(float f) {
     return (uint16_t)(u >> 16);
 }
 
-__device__ __forceinline__ float silu(float z) { return z / (1.0f + __expf(-z)); }
+__device__ __forceinline__ float silu(float z) { return __fdividef(z, 1.0f + __expf(-z)); }
 __device__ __forceinline__ float silu_grad(float z) {
     const float s = 1.0f / (1.0f + __expf(-z));
     return s * (1.0f + z * (1.0f - s));
@@ -449,7 +449,7 @@ __global__ void __launch_bounds__(128) gemm_kernel(int M, int N, int K, const ui
 
 // ---------------------------------------------------------------------------
 // The pipelined form for K a multiple of 64: warp-specialised persistent CTAs
-// of 192 threads.
+// of 320 threads.
 //   warp 0 (one lane)  TMA producer: the weights once (K/64 boxes of
 //                      64 x N, 128-byte swizzle), then per tile K/64 boxes of
 //                      64 x 128 of X into a 4-stage ring (full/empty
@@ -458,9 +458,10 @@ __global__ void __launch_bounds__(128) gemm_kernel(int M, int N, int K, const ui
 //                      start address +32 bytes inside the swizzled 128-byte
 //                      rows), a commit frees the stage; per tile a commit
 //                      hands the accumulator to the epilogue;
-//   warps 2-5          epilogue: tcgen05.ld of their 32-lane quarter of the
-//                      accumulator, bias, SiLU, 16-byte stores, then release
-//                      the accumulator buffer.
+//   warps 2-9          epilogue: tcgen05.ld of their 32-lane quarter of the
+//                      accumulator (two warps per quarter, alternate 16-column
+//                      chunks), bias, SiLU, 16-byte stores, then release the
+//                      accumulator buffer.
 // Two accumulator buffers in tensor memory let the epilogue of one tile run
 // under the MMAs of the next.  Every mbarrier wait is bounded; a wait that
 // runs out raises a CTA-wide abort flag, every role leaves its loop, the
@@ -507,7 +508,7 @@ __device__ __forceinline__ void commit(uint32_t bar) {
                  : "memory");
 }
 
-__global__ void __launch_bounds__(192, 1) gemm_kernel(const __grid_constant__ CUtensorMap map_x,
+__global__ void __launch_bounds__(320, 1) gemm_kernel(const __grid_constant__ CUtensorMap map_x,
                                                       const __grid_constant__ CUtensorMap map_w, int M, int N, int K,
                                                       const float *__restrict__ bias, int act,
                                                       float *__restrict__ Z, void *__restrict__ Y, int ldy,
@@ -537,7 +538,7 @@ __global__ void __launch_bounds__(192, 1) gemm_kernel(const __grid_constant__ CU
         }
         for (int b = 0; b < 2; ++b) {
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar(ACC_FULL + b)) : "memory");
-            asm volatile("mbarrier.init.shared::cta.b64 [%0], 4;\n" ::"r"(bar(ACC_EMPTY + b)) : "memory");
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 8;\n" ::"r"(bar(ACC_EMPTY + b)) : "memory");
         }
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar(W_FULL)) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
@@ -616,8 +617,11 @@ __global__ void __launch_bounds__(192, 1) gemm_kernel(const __grid_constant__ CU
             }
         }
     } else {
-        // epilogue warps 2..5: warp w reads lanes 32 * (w % 4) .. + 31
+        // epilogue warps 2..9: warp w reads lanes 32 * (w % 4) .. + 31 and
+        // every other 16-column chunk (the two warps of a lane quarter split
+        // the columns)
         const int q = warp & 3;
+        const int half = (warp - 2) >> 2;
         const bool vec_ok = (ldy % 8 == 0) && (((uintptr_t)Y & 15u) == 0) && (!Z || ((uintptr_t)Z & 15u) == 0);
         uint32_t t_local = 0;
         for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x, ++t_local) {
@@ -626,7 +630,7 @@ __global__ void __launch_bounds__(192, 1) gemm_kernel(const __grid_constant__ CU
             if (!done) break;
             asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
             const int m = tile * TM + q * 32 + lane;
-            for (int c0 = 0; c0 < n_mma; c0 += 16) {
+            for (int c0 = 16 * half; c0 < n_mma; c0 += 32) {
                 uint32_t r[16];
                 tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + b * buf_cols + (uint32_t)c0, r);
                 if (m >= M) continue;
@@ -784,7 +788,7 @@ extern "C" int mpf3d_gemm_bf16_tc5(int M, int N, int K, const uint16_t *A, int64
                 return MPF3D_ERR_CUDA;
             const int tiles = (M + tc5::TM - 1) / tc5::TM;
             const int grid = tiles < sms_of_device() ? tiles : sms_of_device();
-            tc5::tma::gemm_kernel<<<grid, 192, bytes, (cudaStream_t)stream>>>(mx, mw, M, N, K, bias, act, Z, Y, ldy,
+            tc5::tma::gemm_kernel<<<grid, 320, bytes, (cudaStream_t)stream>>>(mx, mw, M, N, K, bias, act, Z, Y, ldy,
                                                                              y_bf16, beta);
             return cudaGetLastError() == cudaSuccess ? MPF3D_OK : MPF3D_ERR_CUDA;
         }
