@@ -3,8 +3,13 @@
 Workload (default): 256^3 grid, 64 grains seeded uniformly in the bottom 32
 z-layers (3D Voronoi) plus liquid (N = 65 phases), tanh front, anisotropy and
 torque on, uniform cooling, config_3d.yaml physics, 2000 steps -- advanced by
-the compact FP32 fused stepper (one kernel per step).  Synthetic seeded
-inputs of the configured shape; no dataset is involved.
+the compact FP32 stepper (sweep, general and interface kernels per step).
+Synthetic seeded inputs of the configured shape; no dataset is involved.
+
+With --gpus N (one process per GPU under torchrun) every rank advances its own
+replica of the workload and its own share of the bicrystal batch: the work is
+independent, no data crosses ranks, and the timings are the maximum over ranks
+(weak scaling).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -338,11 +343,7 @@ def run_ours(args, rank, world):
         torch.cuda.synchronize(dev)
         barrier()
     solver.check()
-    ms = e0.elapsed_time(e1)
-    if world > 1:
-        t = torch.tensor([ms], dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(e0.elapsed_time(e1), world)
     final_cnt_sum = int(solver.stored_counts().sum(dtype=torch.int64).item())
 
     # accounting pass (untimed), the same run again: per step, the record
@@ -401,8 +402,8 @@ def run_ours(args, rank, world):
         extra["accuracy_fp32_vs_fp64"] = accuracy_run(args, phi0, temp, n111, wij, aij, mij, phys, dev)
     del phi0
     torch.cuda.empty_cache()
-    if rank == 0 and not args.no_bicrystal and args.bicrystal_steps > 0:
-        extra["bicrystal_batch"] = bicrystal_run(args, dev)
+    if not args.no_bicrystal and args.bicrystal_steps > 0:
+        extra["bicrystal_batch"] = bicrystal_run(args, dev, rank, world)
     if rank == 0 and not args.no_gemm:
         extra["surrogate_gemm"] = gemm_run(dev)
     emit(args, rank, world, value, ms, cells, t_e2e, in_bytes, out_bytes, achieved, peak, peak_kind,
@@ -428,10 +429,7 @@ def e2e_run(args, phi0, temp, n111, wij, aij, mij, phys, dev, barrier, world, tu
     t_e2e = time.perf_counter() - t0
     s2.check()
     barrier()
-    if world > 1:
-        t = torch.tensor([t_e2e], dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        t_e2e = float(t.item())
+    t_e2e = max_over_ranks(t_e2e, world)
     in_bytes = phi_host.numel() * 4 + temp.nbytes + n111.nbytes + 3 * wij.nbytes
     out_bytes = out_host.numel() * 4
     return t_e2e, in_bytes, out_bytes
@@ -524,15 +522,53 @@ def accuracy_run(args, phi0, temp, n111, wij, aij, mij, phys, dev):
     return out
 
 
-def bicrystal_run(args, dev):
+def _reduce_scalar(x: float, world: int, op) -> float:
+    if world <= 1:
+        return float(x)
+    import torch
+    dist = torch.distributed
+    # NCCL reduces device tensors only; gloo (the CPU tests) host tensors
+    dev = (torch.device("cuda", torch.cuda.current_device())
+           if dist.get_backend() == "nccl" else torch.device("cpu"))
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=op)
+    return float(t.item())
+
+
+def max_over_ranks(x: float, world: int) -> float:
+    """The largest of every rank's value (a time: the job ends with its
+    slowest rank)."""
+    import torch
+    return _reduce_scalar(x, world, torch.distributed.ReduceOp.MAX if world > 1 else None)
+
+
+def sum_over_ranks(x: float, world: int) -> float:
+    import torch
+    return _reduce_scalar(x, world, torch.distributed.ReduceOp.SUM if world > 1 else None)
+
+
+def shard_range(n: int, rank: int, world: int):
+    """Rank `rank`'s contiguous share [lo, hi) of n independent items (the
+    batched instances shard across GPUs with no exchange)."""
+    base, extra = divmod(n, world)
+    lo = rank * base + min(rank, extra)
+    return lo, lo + base + (1 if rank < extra else 0)
+
+
+def bicrystal_run(args, dev, rank=0, world=1):
     """Batched bicrystals: 512 instances of sizes drawn from {64,96,128}^2 x
     {64,96}, undercooling U[0.25, 3] K, anisotropy strength U[0, 1], random
     orientation pairs, stepped together from CUDA-graph replays; outputs
     velocity ratio and grain-boundary inclination per instance."""
     import torch
     from mpf3d.batched import BatchedBicrystals, sample_batch
-    n = args.bicrystal_instances
-    dims, q, dT, da = sample_batch(n, seed=SEED)
+    # weak scaling: every rank runs its own batch of args.bicrystal_instances
+    # instances, drawn from one sample of world * instances
+    n_all = args.bicrystal_instances * world
+    dims_all, q_all, dT_all, da_all = sample_batch(n_all, seed=SEED)
+    lo, hi = shard_range(n_all, rank, world)
+    dims, q, dT, da = dims_all[lo:hi], q_all[lo:hi], dT_all[lo:hi], da_all[lo:hi]
+    n = hi - lo
     b = BatchedBicrystals(dims, q, dT, da, base_height=16.0, slots=4, device=dev)
     b.capture(50)
     b.step(50)  # warm-up replay
@@ -543,13 +579,14 @@ def bicrystal_run(args, dev):
     t0 = time.perf_counter()
     res = b.run(args.bicrystal_steps, sample_every=100, graph_steps=50)
     torch.cuda.synchronize(dev)
-    wall = time.perf_counter() - t0
+    wall = max_over_ranks(time.perf_counter() - t0, world)
+    cells = sum_over_ranks(b.total_cells, world)
     ratio = res["velocity_ratio"]
     ang = res["gb_angle_deg"]
     fin = np.isfinite(ratio)
-    return {"instances": n, "steps": args.bicrystal_steps, "cells_per_step": b.total_cells,
-            "wall_s": wall, "cases_per_hour": n / wall * 3600.0,
-            "cell_steps_per_s": b.total_cells * args.bicrystal_steps / wall,
+    return {"instances": n_all, "steps": args.bicrystal_steps, "cells_per_step": int(cells),
+            "wall_s": wall, "cases_per_hour": n_all / wall * 3600.0,
+            "cell_steps_per_s": cells * args.bicrystal_steps / wall,
             "velocity_ratio": {"finite": int(fin.sum()),
                                "median": float(np.median(ratio[fin])) if fin.any() else None},
             "gb_inclination_deg": {"finite": int(np.isfinite(ang).sum()),
