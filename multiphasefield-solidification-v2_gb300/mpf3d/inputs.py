@@ -244,3 +244,78 @@ def wavy_front(nx: int, ny: int, nz: int, dz: float, delta: float, base: float, 
     phi[1] = np.broadcast_to(solid, (nx, ny, nz))
     phi[0] = 1.0 - phi[1]
     return phi
+
+
+def _wavy_solid(nx: int, nz: int, dz: float, delta: float, base: float, waviness: float) -> np.ndarray:
+    """[nx, 1, nz] tanh solid fraction under a front at
+    base + waviness*cos(2 pi x/nx)."""
+    x = np.arange(nx, dtype=np.float64).reshape(nx, 1, 1)
+    z = np.arange(nz, dtype=np.float64).reshape(1, 1, nz)
+    h = base + waviness * np.cos(2.0 * math.pi * x / max(nx, 1))
+    return (0.5 * (1.0 - np.tanh(np.float32(2.2 / delta) * ((z - h) * dz)))).astype(np.float32)
+
+
+def stripe_grain_map(nx: int, ny: int, n_solid: int) -> np.ndarray:
+    """[nx, ny] grain ids 1..n_solid in equal x stripes (edges at
+    linspace(0, nx, n_solid+1) truncated), tests/verification_3d.py:296-301."""
+    edges = np.linspace(0, nx, n_solid + 1).astype(int)
+    col = np.zeros(nx, np.int32)
+    for g in range(1, n_solid + 1):
+        col[edges[g - 1]:edges[g]] = g
+    return np.repeat(col[:, None], ny, axis=1)
+
+
+def bicrystal_field(nx: int, ny: int, nz: int, dz: float, delta: float, seed_height: float,
+                    split_index: int, waviness: float = 0.0, left_offset: float = 0.0,
+                    right_offset: float = 0.0) -> np.ndarray:
+    """phi [3, nx, ny, nz] float32: grain 1 for x < split_index, grain 2 from
+    there on, each under its own (optionally wavy) front, liquid the clipped
+    rest; bicrystal_phi_3d, tests/verification_3d.py:1085-1111."""
+    phi = np.zeros((3, nx, ny, nz), np.float32)
+    left = _wavy_solid(nx, nz, dz, delta, seed_height + left_offset, waviness)
+    right = _wavy_solid(nx, nz, dz, delta, seed_height + right_offset, waviness)
+    phi[1, :split_index] = np.broadcast_to(left[:split_index], (split_index, ny, nz))
+    phi[2, split_index:] = np.broadcast_to(right[split_index:], (nx - split_index, ny, nz))
+    phi[0] = np.clip(1.0 - phi[1] - phi[2], 0.0, 1.0)
+    return phi
+
+
+def alternating_multigrain_field(nx: int, ny: int, nz: int, dz: float, delta: float, seed_height: float,
+                                 n_grains: int, waviness: float = 0.0) -> np.ndarray:
+    """Stripes of n_grains grains under one front; with waviness the front
+    is base + waviness*cos(2 pi x/nx) (alternating_multigrain_phi_3d,
+    tests/verification_3d.py:1114-1135)."""
+    gmap = stripe_grain_map(nx, ny, n_grains)
+    phi = phi_from_grain_map_2d(gmap, n_grains, nz, dz, delta, int(seed_height))
+    if waviness == 0.0:
+        return phi
+    solid = _wavy_solid(nx, nz, dz, delta, seed_height, waviness)
+    for g in range(1, n_grains + 1):
+        phi[g] = np.where((gmap == g)[:, :, None], solid, 0.0)
+    phi[0] = np.clip(1.0 - phi[1:].sum(axis=0), 0.0, 1.0)
+    return phi
+
+
+def quaternions_of(rotations) -> np.ndarray:
+    """[len+1, 4] (x, y, z, w): the liquid's identity, then one scipy Rotation
+    per grain (quaternions_from_rotations, tests/verification_3d.py:304-309)."""
+    q = np.zeros((len(rotations) + 1, 4), np.float64)
+    q[0] = (0.0, 0.0, 0.0, 1.0)
+    for g, r in enumerate(rotations, 1):
+        q[g] = r.as_quat()
+    return q
+
+
+def orientation_library() -> dict:
+    """The verification suite's named grain orientations
+    (orientation_library, tests/verification_3d.py:1138-1147)."""
+    from scipy.spatial.transform import Rotation
+    src = np.array([[1.0, 1.0, 1.0]]) / math.sqrt(3.0)
+    aligned, _ = Rotation.align_vectors(np.array([[0.0, 0.0, 1.0]]), src)
+    return {"identity": Rotation.identity(),
+            "y_15": Rotation.from_euler("y", 15.0, degrees=True),
+            "y_30": Rotation.from_euler("y", 30.0, degrees=True),
+            "y_45": Rotation.from_euler("y", 45.0, degrees=True),
+            "x_30": Rotation.from_euler("x", 30.0, degrees=True),
+            "tilt_xyz": Rotation.from_euler("xyz", [20.0, 35.0, 10.0], degrees=True),
+            "aligned_111_to_z": aligned}

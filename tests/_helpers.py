@@ -14,6 +14,8 @@ def golden_files(kind="run"):
     out = []
     for f in sorted(glob.glob(os.path.join(GOLDEN, "*.npz"))):
         g = np.load(f)
+        if "phi0" not in g.files:
+            continue  # analysis fixtures (groove_metrics.npz)
         if "phi" not in g.files:
             k = "apt"
         else:

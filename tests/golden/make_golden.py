@@ -317,6 +317,21 @@ def main():
         run_case_2d(ref, "stripes2d_f64", phis, t2.astype(np.float64), q3, dict(p, p_round=0.02), steps=3,
                     f64=True)
 
+    # Grain-boundary groove: the set-up of groove_depth_only / robust_groove_angle_estimation
+    # (tests/verification_3d.py:2453-2489, 2491-2539): 20x6x24 bicrystal under a front at
+    # 7 + 0.6 cos(2 pi x/nx), isotropic (delta_a 0, ksi 1, both toggles off), G = V = 0,
+    # T_melt, 20 steps.  The reference's recorded groove metrics of this run pin the analysis.
+    if want("groove_f32"):
+        bi = importlib.import_module("bicrystal_reference")
+        pg = dict(p, delta_a=0.0, ksi=1.0, G=0.0, V_pulling=0.0)
+        dg = derived(pg)
+        phig = bi.reference_functions(args.reference)["bicrystal_phi_3d"](
+            20, 6, 24, pg["dx"], dg["delta"], 7.0, 10, waviness=0.6)
+        qg = np.array([[0.0, 0.0, 0.0, 1.0]] * 3)
+        tg = np.full((20, 6, 24), np.float32(pg["T_melt"]), np.float32)
+        run_case(ref, "groove_f32", phig, tg, qg, pg, steps=20, f64=False, aniso=0, torque=0,
+                 cooling=False)
+
     # APT known answers: boundary probes and the crafted KMAX overflow
     # (tests/verification_3d.py:1459-1480, 1538-1565).
     if want("apt_boundary"):
