@@ -400,6 +400,7 @@ def run_ours(args, rank, world):
         del solver
         torch.cuda.empty_cache()
         extra["accuracy_fp32_vs_fp64"] = accuracy_run(args, phi0, temp, n111, wij, aij, mij, phys, dev)
+        extra["accuracy_fp32_vs_fp64"]["groove_and_bicrystal"] = groove_accuracy(dev)
     del phi0
     torch.cuda.empty_cache()
     if not args.no_bicrystal and args.bicrystal_steps > 0:
@@ -433,6 +434,83 @@ def e2e_run(args, phi0, temp, n111, wij, aij, mij, phys, dev, barrier, world, tu
     in_bytes = phi_host.numel() * 4 + temp.nbytes + n111.nbytes + 3 * wij.nbytes
     out_bytes = out_host.numel() * 4
     return t_e2e, in_bytes, out_bytes
+
+
+def _dense_run(phi0, temp_value, quats, phys, steps, aniso, torque, f64, dev):
+    """The reference harness's step sequence on the drop-in kernels: FP64
+    (float64 phi, temperature and scalars) or the reference's own float32
+    typing."""
+    import torch
+    from mpf3d import inputs
+    from src import gpu_kernels_3d as K
+    N, nx, ny, nz = phi0.shape
+    dt = np.float64 if f64 else np.float32
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+    p, q = t(phi0.astype(dt)), t(phi0.astype(dt))
+    T = t(np.full((nx, ny, nz), dt(temp_value), dt))
+    mf = torch.zeros((50, nx, ny, nz), dtype=torch.int32, device=dev)
+    nf = torch.zeros((nx, ny, nz), dtype=torch.int32, device=dev)
+    wij, aij, mij = inputs.matrices_for(phys, N)
+    W, A, M, U = t(wij), t(aij), t(mij), t(inputs.rotated_n111(quats))
+    sc = phys.kernel_scalars(f32=not f64)
+    rate = dt(phys.derived()["cooling_rate"])
+    cfg = ((-(-nx // 4), -(-ny // 4), -(-nz // 4)), (4, 4, 4))
+    for _ in range(steps):
+        if float(rate) != 0.0:
+            K.kernel_update_temp_3d[cfg](T, rate, nx, ny, nz)
+        K.kernel_update_nfmf_3d[cfg](p, mf, nf, nx, ny, nz, N)
+        K.kernel_update_phasefield_active_3d_switchable[cfg](p, q, T, mf, nf, W, A, M, U, nx, ny, nz, N, *sc,
+                                                             np.int32(aniso), np.int32(torque))
+        p, q = q, p
+    torch.cuda.synchronize(dev)
+    K.check_errors()
+    return p.cpu().numpy()
+
+
+def groove_accuracy(dev):
+    """Groove and bicrystal observables (mpf3d.groove: the reference's
+    robust_groove_metrics and bicrystal_group_metrics,
+    tests/verification_3d.py:571-609, 1366-1381) of FP32 runs against FP64:
+      groove     -- the groove_depth_only set-up (20x6x24 bicrystal, isotropic,
+                    20 steps at T_melt, tests/verification_3d.py:2453-2488);
+      bicrystal  -- the kinetic-regime set-up (18x6x28, aligned{111} | identity,
+                    delta_a 0.35, ksi 0.01, 6 K undercooling, 10 steps,
+                    :2326-2385)."""
+    from scipy.spatial.transform import Rotation
+    from mpf3d import groove, inputs
+    from mpf3d.solver import CompactSolver
+    lib = inputs.orientation_library()
+    setups = {
+        "groove": (inputs.Physics(delta_a=0.0, ksi=1.0, G=0.0, V_pulling=0.0), (20, 6, 24), 10, 0.6, 20,
+                   0.0, inputs.quaternions_of([Rotation.identity()] * 2), 0),
+        "bicrystal": (inputs.Physics(delta_a=0.35, ksi=0.01, p_round=0.02, G=0.0, V_pulling=0.0), (18, 6, 28), 9,
+                      0.8, 10, 6.0, inputs.quaternions_of([lib["aligned_111_to_z"], lib["identity"]]), 1),
+    }
+    out = {}
+    for name, (phys, (nx, ny, nz), split, wav, steps, dT, q, aniso) in setups.items():
+        phi0 = inputs.bicrystal_field(nx, ny, nz, phys.dx, phys.derived()["delta"], 7.0, split, waviness=wav)
+        root0 = groove.grain_boundary_root(phi0, 1, 2, x_guess=split)["root_x_cells"]
+        T = phys.T_melt - dT
+        runs = {"fp64": _dense_run(phi0, T, q, phys, steps, aniso, 0, True, dev),
+                "f32_reference_numerics": _dense_run(phi0, T, q, phys, steps, aniso, 0, False, dev)}
+        wij, aij, mij = inputs.matrices_for(phys, 3)
+        c = CompactSolver(phi0, np.full(nz, T), inputs.rotated_n111(q), wij, aij, mij, phys,
+                          anisotropy=bool(aniso), torque=False, device=dev)
+        c.step(steps)
+        runs["fp32_compact"] = c.to_dense(np.float32)
+        rec = {}
+        for k, phi in runs.items():
+            gm = groove.groove_metrics(phi, root_x_guess=float(split))
+            fam = groove.family_volumes(phi, [1], [2], phys.dx)
+            rec[k] = {"dihedral_angle_like_deg": gm["dihedral_angle_like_deg"],
+                      "root_z_cells": gm["root_z_cells"], "groove_depth_cells": gm["groove_depth_cells"],
+                      "root_shift_cells": gm["root_x_cells"] - root0,
+                      "winner_loser_volume_ratio": fam["winner_loser_volume_ratio"],
+                      "max_abs_dphi_vs_fp64": float(np.abs(phi.astype(np.float64) - runs["fp64"]).max())}
+        for k in ("f32_reference_numerics", "fp32_compact"):
+            rec[k]["dihedral_diff_deg"] = rec[k]["dihedral_angle_like_deg"] - rec["fp64"]["dihedral_angle_like_deg"]
+        out[name] = rec
+    return out
 
 
 def interface_height(phi_liquid):

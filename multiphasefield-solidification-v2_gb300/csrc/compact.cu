@@ -577,11 +577,72 @@ __device__ __forceinline__ void push(const Queue &Q, int parity, bool want, int 
 
 constexpr int SWEEP_ZB = 4;  // cells per thread along z (default; batches always use it)
 
+// Where the sweep sends a queued cell: list 0 (general), 1 (interface) or 2
+// (interface with several solids).  DirectSink appends at once, with one
+// global atomic per warp and list; BlockSink only counts in shared memory
+// and keeps each cell's list and offset in registers, so that the block
+// reserves its segments with one global atomic per list (flush) -- the
+// counters are one address each, and per-warp atomics from every SM queue up
+// at the L2 slice that holds them.  Cells are independent, so the order of a
+// list does not change any result.
+struct DirectSink {
+    const Queue &Q;
+    int parity;
+    uint32_t cells;
+    __device__ __forceinline__ void add(int, int list, uint32_t c) {
+        push(Q, parity, list == 1, 1, cells, c);
+        push(Q, parity, list == 2, 2, cells, c);
+        push(Q, parity, list == 0, 0, cells, c);
+    }
+};
+
+template <int ZB>
+struct BlockSink {
+    uint32_t *cnt;     // shared: cells of the block per list
+    uint32_t off[ZB];  // cell j's position in its list's block segment
+    int lst[ZB];       // cell j's list, -1 if it is not queued
+
+    __device__ __forceinline__ explicit BlockSink(uint32_t *c) : cnt(c) {
+#pragma unroll
+        for (int j = 0; j < ZB; ++j) {
+            off[j] = 0;
+            lst[j] = -1;
+        }
+    }
+    __device__ __forceinline__ void add(int j, int list, uint32_t) {
+        const unsigned am = __activemask();
+        const int lane = threadIdx.x & 31;
+#pragma unroll
+        for (int L = 0; L < 3; ++L) {
+            const unsigned bm = __ballot_sync(am, list == L);
+            if (!bm) continue;
+            const int leader = __ffs(bm) - 1;
+            uint32_t base = 0;
+            if (lane == leader) base = atomicAdd(cnt + L, (uint32_t)__popc(bm));
+            base = __shfl_sync(am, base, leader);
+            if (list == L) off[j] = base + (uint32_t)__popc(bm & ((1u << lane) - 1u));
+        }
+        lst[j] = list;
+    }
+    // after the block's adds and a barrier: base[L] is the block's first
+    // position in list L; cell j is (k0 + j) * plane + col
+    __device__ __forceinline__ void flush(const Queue &Q, uint32_t cells, const uint32_t *base, uint32_t plane,
+                                          uint32_t col, int k0) const {
+#pragma unroll
+        for (int j = 0; j < ZB; ++j) {
+            if (lst[j] < 0) continue;
+            const uint32_t pos = base[lst[j]] + off[j];
+            const uint32_t c = (uint32_t)(k0 + j) * plane + col;
+            Q.items[lst[j] == 0 ? pos : (lst[j] == 1 ? cells - 1u - pos : cells + pos)] = c;
+        }
+    }
+};
+
 // The sweep of one column of ZB cells (l, m, k0..k0+ZB-1) of a domain;
 // returns whether every one of them was uniform (cells past the top count
 // as uniform).
-template <int ZB = SWEEP_ZB>
-__device__ __forceinline__ bool sweep_column(const In &in, const Out &out, const Params &P, const Queue &Q, int parity,
+template <int ZB = SWEEP_ZB, class Sink>
+__device__ __forceinline__ bool sweep_column(const In &in, const Out &out, const Params &P, bool split, Sink &sink,
                                              int l, int m, int k0) {
     const uint32_t plane = (uint32_t)P.nx * (uint32_t)P.ny;
     const uint32_t col = P.base + (uint32_t)m * (uint32_t)P.nx + (uint32_t)l;
@@ -628,7 +689,7 @@ __device__ __forceinline__ bool sweep_column(const In &in, const Out &out, const
             all_uniform = false;
             const bool heavy = liq && sol && P.use_aniso;
             bool multi = false;
-            if (heavy && Q.split) {
+            if (heavy && split) {
                 // several solids in the active list: a head with 3+ phases or
                 // two solids, or two different solid first ids
                 int sid = -1;
@@ -643,9 +704,7 @@ __device__ __forceinline__ bool sweep_column(const In &in, const Out &out, const
                     }
                 }
             }
-            push(Q, parity, heavy && !multi, 1, P.cells32, c);
-            push(Q, parity, heavy && multi, 2, P.cells32, c);
-            push(Q, parity, !heavy, 0, P.cells32, c);
+            sink.add(j, heavy ? (multi ? 2 : 1) : 0, c);
         }
     }
     return all_uniform;
@@ -675,37 +734,62 @@ __host__ __device__ __forceinline__ uint32_t tiles_of(int nx, int ny, int nz) {
 template <int S, int AMAX, int ZB = SWEEP_ZB>
 __global__ void __launch_bounds__(512) sweep_kernel(In in, Out out, Mats M, Params P, Queue Q, int parity,
                                                     Tiles T, int32_t *__restrict__ err) {
+    __shared__ uint32_t s_cnt[3], s_base[3];
     const int l = blockIdx.x * blockDim.x + threadIdx.x;
     const int m = blockIdx.y * blockDim.y + threadIdx.y;
     const int k0 = (blockIdx.z * blockDim.z + threadIdx.z) * ZB;
+    const int tlin = threadIdx.x + (int)blockDim.x * threadIdx.y;  // blockDim.z is 1
+    if (tlin < 3) s_cnt[tlin] = 0;
     if (blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.x < 2 && threadIdx.y == 0 &&
         threadIdx.z == 0)
         Q.count[2 * (parity ^ 1) + threadIdx.x] = 0;  // the previous step's kernels are done with them
     if (blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.x == 2 && threadIdx.y == 0 &&
         threadIdx.z == 0 && Q.split)
         Q.count[4 + (parity ^ 1)] = 0;
-    // a warp is one threadIdx.y row: its 32 lanes share m and k0
-    if (m >= P.ny || k0 >= P.nz) return;
-    if (!T.flags) {
-        if (l < P.nx) sweep_column<ZB>(in, out, P, Q, parity, l, m, k0);
-        return;
+    __syncthreads();
+    BlockSink<ZB> sink(s_cnt);
+    // a warp is one threadIdx.y row: its 32 lanes share m and k0, so every
+    // branch below is warp-uniform except l < nx
+    if (m < P.ny && k0 < P.nz) {
+        if (!T.flags) {
+            if (l < P.nx) sweep_column<ZB>(in, out, P, Q.split, sink, l, m, k0);
+        } else {
+            const int tx = (int)blockIdx.x, kb = k0 / ZB;
+            const uint8_t *fin = T.flags + (size_t)(parity ^ 1) * T.n;
+            uint8_t *fout = T.flags + (size_t)parity * T.n;
+            auto tid = [&](int a, int b, int c) {
+                return ((uint32_t)c * (uint32_t)P.ny + (uint32_t)b) * (uint32_t)T.ntx + a;
+            };
+            const uint32_t t = tid(tx, m, kb);
+            // the 7 flags are loaded together (no short-circuit chain of loads)
+            const uint32_t f0 = fin[t];
+            const uint32_t f1 = fin[tid(tx + 1 < T.ntx ? tx + 1 : 0, m, kb)];
+            const uint32_t f2 = fin[tid(tx > 0 ? tx - 1 : T.ntx - 1, m, kb)];
+            const uint32_t f3 = fin[tid(tx, m + 1 < P.ny ? m + 1 : 0, kb)];
+            const uint32_t f4 = fin[tid(tx, m > 0 ? m - 1 : P.ny - 1, kb)];
+            const uint32_t f5 = fin[tid(tx, m, kb + 1 < T.nkb ? kb + 1 : kb)];
+            const uint32_t f6 = fin[tid(tx, m, kb > 0 ? kb - 1 : kb)];
+            const bool quiet = (f0 & f1 & f2 & f3 & f4 & f5 & f6) != 0u;
+            const bool lane0 = (threadIdx.x & 31) == 0;
+            if (quiet) {
+                if (lane0) fout[t] = 1;
+            } else {
+                const bool uni = l < P.nx ? sweep_column<ZB>(in, out, P, Q.split, sink, l, m, k0) : true;
+                const bool all = __all_sync(0xffffffffu, uni);
+                if (lane0) fout[t] = all ? 1 : 0;
+            }
+        }
     }
-    const int tx = (int)blockIdx.x, kb = k0 / ZB;
-    const uint8_t *fin = T.flags + (size_t)(parity ^ 1) * T.n;
-    uint8_t *fout = T.flags + (size_t)parity * T.n;
-    auto tid = [&](int a, int b, int c) { return ((uint32_t)c * (uint32_t)P.ny + (uint32_t)b) * (uint32_t)T.ntx + a; };
-    const uint32_t t = tid(tx, m, kb);
-    const bool quiet = fin[t] && fin[tid(tx + 1 < T.ntx ? tx + 1 : 0, m, kb)] && fin[tid(tx > 0 ? tx - 1 : T.ntx - 1, m, kb)] &&
-                       fin[tid(tx, m + 1 < P.ny ? m + 1 : 0, kb)] && fin[tid(tx, m > 0 ? m - 1 : P.ny - 1, kb)] &&
-                       fin[tid(tx, m, kb + 1 < T.nkb ? kb + 1 : kb)] && fin[tid(tx, m, kb > 0 ? kb - 1 : kb)];
-    const bool lane0 = (threadIdx.x & 31) == 0;
-    if (quiet) {
-        if (lane0) fout[t] = 1;
-        return;
+    __syncthreads();
+    if (tlin < 3) {
+        const uint32_t n = s_cnt[tlin];
+        uint32_t *ctr = tlin == 2 ? Q.count + 4 + parity : Q.count + 2 * parity + tlin;
+        s_base[tlin] = n ? atomicAdd(ctr, n) : 0u;
     }
-    const bool uni = l < P.nx ? sweep_column<ZB>(in, out, P, Q, parity, l, m, k0) : true;
-    const bool all = __all_sync(0xffffffffu, uni);
-    if (lane0) fout[t] = all ? 1 : 0;
+    __syncthreads();
+    if (l < P.nx && m < P.ny && k0 < P.nz)
+        sink.flush(Q, P.cells32, s_base, (uint32_t)P.nx * (uint32_t)P.ny,
+                   P.base + (uint32_t)m * (uint32_t)P.nx + (uint32_t)l, k0);
 }
 
 // Kernel 2 of a step: the cells queued for the general update, one thread
@@ -861,7 +945,8 @@ __global__ void __launch_bounds__(256) batched_sweep_kernel(In in, Out out, Para
     const int k0 = (t / (tx * ty)) * SWEEP_ZB;
     if (l >= I.nx || m >= I.ny || k0 >= I.nz) return;
     const Params P = instance_params(P0, I);
-    sweep_column(in, out, P, Q, parity, l, m, k0);
+    DirectSink sink{Q, parity, P.cells32};
+    sweep_column(in, out, P, Q.split, sink, l, m, k0);
 }
 
 template <int S, int AMAX, bool HEAVY>
