@@ -559,42 +559,16 @@ __device__ __forceinline__ void process_cell(const In &in, const Out &out, const
 // (liquid and a solid in the neighbourhood, anisotropy on) to the back,
 // the rest (grain boundaries, junctions without liquid, the isotropic model)
 // to the front -- so that the general update runs with converged warps.
-__device__ __forceinline__ void push(const Queue &Q, int parity, bool want, int list, uint32_t cells, uint32_t c) {
-    const unsigned am = __activemask();
-    const unsigned bm = __ballot_sync(am, want);
-    if (!bm) return;
-    const int lane = threadIdx.x & 31;
-    const int leader = __ffs(bm) - 1;
-    uint32_t base = 0;
-    uint32_t *ctr = list == 2 ? Q.count + 4 + parity : Q.count + 2 * parity + list;
-    if (lane == leader) base = atomicAdd(ctr, (uint32_t)__popc(bm));
-    base = __shfl_sync(am, base, leader);
-    if (want) {
-        const uint32_t pos = base + __popc(bm & ((1u << lane) - 1u));
-        Q.items[list == 0 ? pos : (list == 1 ? cells - 1u - pos : cells + pos)] = c;
-    }
-}
-
 constexpr int SWEEP_ZB = 4;  // cells per thread along z (default; batches always use it)
 
 // Where the sweep sends a queued cell: list 0 (general), 1 (interface) or 2
-// (interface with several solids).  DirectSink appends at once, with one
-// global atomic per warp and list; BlockSink only counts in shared memory
-// and keeps each cell's list and offset in registers, so that the block
-// reserves its segments with one global atomic per list (flush) -- the
-// counters are one address each, and per-warp atomics from every SM queue up
-// at the L2 slice that holds them.  Cells are independent, so the order of a
-// list does not change any result.
-struct DirectSink {
-    const Queue &Q;
-    int parity;
-    uint32_t cells;
-    __device__ __forceinline__ void add(int, int list, uint32_t c) {
-        push(Q, parity, list == 1, 1, cells, c);
-        push(Q, parity, list == 2, 2, cells, c);
-        push(Q, parity, list == 0, 0, cells, c);
-    }
-};
+// (interface with several solids).  BlockSink counts a block's cells per
+// list in shared memory (one shared atomic per warp, cell and list) and
+// keeps each cell's list and offset in registers; the block then reserves
+// its segments with one global atomic per list and writes the cell indices
+// (flush).  The counters are one address each, and per-warp global atomics
+// from every SM queued up at the L2 slice that holds them.  Cells are
+// independent, so the order within a list changes no result.
 
 template <int ZB>
 struct BlockSink {
@@ -934,8 +908,13 @@ template <int S, int AMAX>
 __global__ void __launch_bounds__(256) batched_sweep_kernel(In in, Out out, Params P0,
                                                             const mpf3d_instance *__restrict__ inst, int n_inst,
                                                             Queue Q, int parity) {
+    __shared__ uint32_t s_cnt[3], s_base[3];
+    const int tlin = threadIdx.x + 32 * threadIdx.y;
+    if (tlin < 3) s_cnt[tlin] = 0;
     if (blockIdx.x == 0 && threadIdx.x < 2 && threadIdx.y == 0) Q.count[2 * (parity ^ 1) + threadIdx.x] = 0;
     if (blockIdx.x == 0 && threadIdx.x == 2 && threadIdx.y == 0 && Q.split) Q.count[4 + (parity ^ 1)] = 0;
+    __syncthreads();
+    // one block is one tile of one instance
     const int i = find_instance_by_tile(inst, n_inst, (int)blockIdx.x);
     const mpf3d_instance I = inst[i];
     const int t = (int)blockIdx.x - I.tile_start;
@@ -943,10 +922,20 @@ __global__ void __launch_bounds__(256) batched_sweep_kernel(In in, Out out, Para
     const int l = (t % tx) * 32 + threadIdx.x;
     const int m = ((t / tx) % ty) * 8 + threadIdx.y;
     const int k0 = (t / (tx * ty)) * SWEEP_ZB;
-    if (l >= I.nx || m >= I.ny || k0 >= I.nz) return;
+    const bool inside = l < I.nx && m < I.ny && k0 < I.nz;
     const Params P = instance_params(P0, I);
-    DirectSink sink{Q, parity, P.cells32};
-    sweep_column(in, out, P, Q.split, sink, l, m, k0);
+    BlockSink<SWEEP_ZB> sink(s_cnt);
+    if (inside) sweep_column(in, out, P, Q.split, sink, l, m, k0);
+    __syncthreads();
+    if (tlin < 3) {
+        const uint32_t n = s_cnt[tlin];
+        uint32_t *ctr = tlin == 2 ? Q.count + 4 + parity : Q.count + 2 * parity + tlin;
+        s_base[tlin] = n ? atomicAdd(ctr, n) : 0u;
+    }
+    __syncthreads();
+    if (inside)
+        sink.flush(Q, P.cells32, s_base, (uint32_t)P.nx * (uint32_t)P.ny,
+                   P.base + (uint32_t)m * (uint32_t)P.nx + (uint32_t)l, k0);
 }
 
 template <int S, int AMAX, bool HEAVY>
