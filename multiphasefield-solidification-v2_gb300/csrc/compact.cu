@@ -132,11 +132,53 @@ __device__ __forceinline__ float calc_a(const Params &P, float c) {
     return P.mu_a * (1.0f + P.delta_a * (C + P.tan_a0 * S));
 }
 
-// b(theta) (calc_b_from_cos :33-55)
-__device__ __forceinline__ float calc_b(const Params &P, float c) {
-    c = fminf(fmaxf(c, -1.0f), 1.0f);
-    if (c <= P.cos_theta_lo) return 1.0f;  // theta >= theta_c: outside the cusp
-    float theta = acosf(c);
+// a * b - c * d with one rounding error at most (Kahan's difference of
+// products); the _rn intrinsics keep the compiler from contracting the
+// error-free steps into other FMAs
+__device__ __forceinline__ float diff_of_products(float a, float b, float c, float d) {
+    const float w = __fmul_rn(c, d);
+    const float e = fmaf(-c, d, w);
+    const float f = fmaf(a, b, -w);
+    return __fadd_rn(f, e);
+}
+
+// theta = acos(c) for the facet's best |cos| c = |g . n| / |g| against the
+// float32 normal n, accurate where c is near 1.  There FP32 acos of a
+// rounded c loses most of theta (an absolute error of 1e-7 in c is a
+// relative error of 1e-7 / theta^2 in 1 - c), and b(theta) is steep.  The
+// reference evaluates c in float64 from the same float32 normals, whose
+// length differs from 1 by their rounding, so
+//   1 - c = (1 - |n|) + |n| (1 - cos t),  t the angle between g and n,
+// with 1 - |n|^2 from compensated squares (TwoProduct, TwoSum) and
+//   1 - cos t = |g x n|^2 / (|g|^2 |n|^2 (1 + cos t))
+// from accurate cross-product components; theta = 2 asin(sqrt((1 - c)/2)).
+// |theta - acos(c)| stays within a few 1e-6 rad against float64 (c > 1,
+// possible when |n| > 1, gives theta = 0 as the reference's clamp does).
+__device__ __forceinline__ float facet_angle(float3 g, const Facet &f) {
+    const float nx = f.nx, ny = f.ny, nz = f.nz;
+    const float p1 = __fmul_rn(nx, nx), e1 = fmaf(nx, nx, -p1);
+    const float p2 = __fmul_rn(ny, ny), e2 = fmaf(ny, ny, -p2);
+    const float p3 = __fmul_rn(nz, nz), e3 = fmaf(nz, nz, -p3);
+    const float s1 = __fadd_rn(p1, p2);
+    const float t1 = __fsub_rn(s1, p1);
+    float err = __fadd_rn(__fsub_rn(p1, __fsub_rn(s1, t1)), __fsub_rn(p2, t1));
+    const float s2 = __fadd_rn(s1, p3);
+    const float t2 = __fsub_rn(s2, s1);
+    err = __fadd_rn(err, __fadd_rn(__fsub_rn(s1, __fsub_rn(s2, t2)), __fsub_rn(p3, t2)));
+    const float dn2 = __fsub_rn(__fsub_rn(1.0f, s2), __fadd_rn(err, __fadd_rn(e1, __fadd_rn(e2, e3))));  // 1 - |n|^2
+    const float cx = diff_of_products(g.y, nz, g.z, ny);
+    const float cy = diff_of_products(g.z, nx, g.x, nz);
+    const float cz = diff_of_products(g.x, ny, g.y, nx);
+    const float sin2 = (cx * cx + cy * cy + cz * cz) / (f.q * (1.0f - dn2));
+    const float omc = fmaxf(0.5f * dn2 + sin2 / (1.0f + f.cabs), 0.0f);  // 1 - c
+    return 2.0f * asinf(sqrtf(0.5f * omc));
+}
+
+// b(theta) (calc_b_from_cos :33-55) for the facet of the liquid gradient g
+// at the cell; below the gradient floor the best cos is 0 and b is 1
+__device__ __forceinline__ float calc_b(const Params &P, float3 g, const Facet &f) {
+    if (!f.valid || f.cabs <= P.cos_theta_lo) return 1.0f;  // theta >= theta_c: outside the cusp
+    const float theta = facet_angle(g, f);
     if (theta >= P.theta_c) return 1.0f;
     const float hp = 1.57079632679489662f;
     float y = hp * (theta / P.theta_c);
@@ -363,7 +405,7 @@ __device__ __forceinline__ void interface_terms(const Params &P, const float3 (&
         lv += P.eps0sq * (Ex + Ey + Ez);
     }
     lap_sl = lv;
-    b_sl = calc_b(P, F[0].cabs);
+    b_sl = calc_b(P, G[0], F[0]);
 }
 
 // Update of one cell whose neighbourhood is not uniform.  HEAVY enables the
