@@ -747,8 +747,10 @@ __host__ __device__ __forceinline__ uint32_t tiles_of(int nx, int ny, int nz) {
     return (uint32_t)((nz + ZB - 1) / ZB) * (uint32_t)ny * (uint32_t)((nx + 31) / 32);
 }
 
+// 40 registers (3 blocks of 512 per SM): more resident warps beat keeping
+// ZB = 8 columns in registers; the tuner then prefers ZB = 4
 template <int S, int AMAX, int ZB = SWEEP_ZB>
-__global__ void __launch_bounds__(512) sweep_kernel(In in, Out out, Mats M, Params P, Queue Q, int parity,
+__global__ void __launch_bounds__(512, 3) sweep_kernel(In in, Out out, Mats M, Params P, Queue Q, int parity,
                                                     Tiles T, int32_t *__restrict__ err) {
     __shared__ uint32_t s_cnt[3], s_base[3];
     const int l = blockIdx.x * blockDim.x + threadIdx.x;
