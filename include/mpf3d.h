@@ -198,7 +198,7 @@ int mpf3d_compact_step_tuned(const uint32_t *head, const uint16_t *idx, const fl
                              void *stream, const mpf3d_tuning *tuning, uint8_t *tile_flags, int options);
 
 /* options of mpf3d_compact_step_tuned */
-#define MPF3D_STEP_MULTI_LIST 1 /* interface cells whose neighbourhood holds two or more solids (judged
+#define MPF3D_STEP_MULTI_LIST 1 /* interface cells whose neighbourhood holds two or more solids (decided
                                  * from the heads) get a work list of their own at
                                  * work_items[cells .. 2*cells): work_items must then hold 2*cells
                                  * entries and work_count 6.  Same results, fewer idle lanes. */

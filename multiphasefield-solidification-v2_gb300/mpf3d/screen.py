@@ -2,7 +2,7 @@
 
 A batch of candidate grain pairs (two orientations, undercooling, anisotropy
 strength) is ranked by the surrogate; the plain FP32 batched solver then
-re-simulates the top-k plus a random audit sample, which both judges the
+re-simulates the top-k plus a random audit sample, which both checks the
 ranking and serves as the fallback answer.  The reference's counterpart is the
 serial scan of run_orientation_scan_3d.py:686-841, which simulates every
 candidate.
