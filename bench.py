@@ -401,6 +401,8 @@ def run_ours(args, rank, world):
         torch.cuda.empty_cache()
         extra["accuracy_fp32_vs_fp64"] = accuracy_run(args, phi0, temp, n111, wij, aij, mij, phys, dev)
         extra["accuracy_fp32_vs_fp64"]["groove_and_bicrystal"] = groove_accuracy(dev)
+    if rank == 0 and not args.no_dense_reference:
+        extra["reference_numerics_dense_gb300"] = dense_reference_rate(phi0, temp, n111, wij, aij, mij, phys, dev)
     del phi0
     torch.cuda.empty_cache()
     if not args.no_bicrystal and args.bicrystal_steps > 0:
@@ -443,6 +445,52 @@ def e2e_run(args, phi0, temp, n111, wij, aij, mij, phys, dev, barrier, world, tu
     in_bytes = phi_host.numel() * 4 + temp.nbytes + n111.nbytes + 3 * wij.nbytes
     out_bytes = out_host.numel() * 4
     return t_e2e, in_bytes, out_bytes
+
+
+def dense_reference_rate(phi0, temp, n111, wij, aij, mij, phys, dev, steps=20):
+    """The same 256^3 workload on the drop-in kernels: the reference's own
+    algorithm, dense [N][nx][ny][nz] layout and float32 typing, in the step
+    sequence of run_randommode_3d.py:267-287 (temperature, APT, update,
+    swap), timed with CUDA events.  The reference's Numba kernels cannot run
+    where numba is absent; this is the same arithmetic on the same GPU."""
+    import torch
+    from src import gpu_kernels_3d as K
+    N, nx, ny, nz = phi0.shape
+    p = phi0.clone()
+    q = torch.empty_like(p)
+    T = torch.from_numpy(np.ascontiguousarray(np.broadcast_to(np.asarray(temp, np.float32), (nx, ny, nz)))).to(dev)
+    mf = torch.zeros((50, nx, ny, nz), dtype=torch.int32, device=dev)
+    nf = torch.zeros((nx, ny, nz), dtype=torch.int32, device=dev)
+    W, A, M, U = (torch.from_numpy(np.ascontiguousarray(a)).to(dev) for a in (wij, aij, mij, n111))
+    sc = phys.kernel_scalars(f32=True)
+    rate = np.float32(phys.derived()["cooling_rate"])
+    cfg = ((-(-nx // 4), -(-ny // 4), -(-nz // 4)), (4, 4, 4))
+    stream = torch.cuda.current_stream(dev)
+
+    def step():
+        nonlocal p, q
+        K.kernel_update_temp_3d[cfg](T, rate, nx, ny, nz)
+        K.kernel_update_nfmf_3d[cfg](p, mf, nf, nx, ny, nz, N)
+        K.kernel_update_phasefield_active_3d[cfg](p, q, T, mf, nf, W, A, M, U, nx, ny, nz, N, *sc)
+        p, q = q, p
+
+    for _ in range(3):
+        step()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize(dev)
+    e0.record(stream)
+    for _ in range(steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    K.check_errors()
+    ms = e0.elapsed_time(e1) / steps
+    out = {"cell_steps_per_s": nx * ny * nz / (ms * 1e-3), "ms_per_step": ms, "steps": steps,
+           "kernels": "drop-in src/gpu_kernels_3d.py: temperature, APT, kernel_update_phasefield_active_3d",
+           "typing": "float32 phi and scalars, float64 arithmetic (the reference's compiled-Numba typing)"}
+    del p, q, T, mf, nf
+    torch.cuda.empty_cache()
+    return out
 
 
 def _dense_run(phi0, temp_value, quats, phys, steps, aniso, torque, f64, dev):
@@ -788,6 +836,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end run (profiling)")
     ap.add_argument("--no-autotune", action="store_true", help="use the default launch shape")
     ap.add_argument("--no-gemm", action="store_true", help="skip the surrogate GEMM measurement")
+    ap.add_argument("--no-dense-reference", action="store_true",
+                    help="skip timing the reference-numerics dense kernels on the same workload")
     ap.add_argument("--grid", type=int, nargs=3, default=None,
                     help="override the 256^3 grid (smaller cases for profiling)")
     ap.add_argument("--accuracy-steps", type=int, default=100)
