@@ -847,6 +847,8 @@ def main():
     ap.add_argument("--no-bicrystal", action="store_true")
     ap.add_argument("--candidates", type=int, default=65536)
     ap.add_argument("--exhaustive", action="store_true", help="c5: also simulate every candidate")
+    ap.add_argument("--screen-rounds", type=int, default=2, help="c5: surrogate refit rounds")
+    ap.add_argument("--recheck", type=int, default=1024, help="c5: candidates re-simulated per refit round")
     args = ap.parse_args()
     global GRID
     if args.grid:
@@ -866,7 +868,8 @@ def main():
         run_accuracy_study(args)
     elif args.workload == "c5":
         from mpf3d.screen import screen
-        rep = screen(n_candidates=args.candidates, exhaustive=args.exhaustive, seed=SEED)
+        rep = screen(n_candidates=args.candidates, exhaustive=args.exhaustive, seed=SEED,
+                     rounds=args.screen_rounds, recheck=args.recheck)
         print(json.dumps({"workload": "surrogate-screened orientation scan", **rep}), flush=True)
     else:
         run_ours(args, rank, world)
