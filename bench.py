@@ -292,7 +292,7 @@ def run_reference(args, rank):
 def config_dict(args):
     return {"workload": "3D random Voronoi 256^3, 64 grains in the bottom 32 z-layers + liquid "
                         "(N=65), tanh front, anisotropy+torque on, uniform cooling (config_3d.yaml), "
-                        "FP32 compact fused step",
+                        "FP32 compact three-kernel step",
             "grid": list(GRID), "phases": N_GRAINS + 1, "slots": args.slots, "steps": args.steps,
             "l2": "inputs larger than L2 (compact state > 129 MB per step)",
             "parallelism": f"replicas x{args.gpus}" if args.gpus > 1 else "single GPU"}

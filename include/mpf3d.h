@@ -105,7 +105,7 @@ int mpf2d_dense_update(const void *phi, void *phi_new, int phi_dtype, const void
 int mpf2d_dense_temp(void *temp, int temp_dtype, double cooling_rate, int rate_is_f32, int nx, int ny,
                      void *stream);
 
-/* ---- compact FP32 tier (fused step) -------------------------------------
+/* ---- compact FP32 tier (three-kernel step) -------------------------------
  * State of one buffer (x fastest: cell = (k*ny + m)*nx + l):
  *   head uint32[cells]        bits 0-6 number n of stored phases (phi > 0),
  *                             bit 7 single value stored explicitly,

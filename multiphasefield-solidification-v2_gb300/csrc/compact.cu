@@ -1259,8 +1259,8 @@ Params shared_params(const mpf3d_scalars *sc, int enable_anisotropy, int enable_
     P.g2_floor = (float)v[MPF3D_S_G2_FLOOR];
     P.ksi = (float)v[MPF3D_S_KSI];
     P.theta_c = (float)v[MPF3D_S_THETA_C_RAD];
-    // below this cosine acosf(c) >= theta_c holds with margin (acosf is
-    // within a few ulp; the margin is ~1e-5 rad), so b = 1 without acosf
+    // below this best |cos| the facet angle is >= theta_c with a margin far
+    // above the FP32 error of c (~1e-7), so b = 1 without computing the angle
     P.cos_theta_lo = (float)(cos(v[MPF3D_S_THETA_C_RAD]) - 1.0e-5);
     P.Sf = (float)v[MPF3D_S_SF];
     P.Tmc = v[MPF3D_S_T_MELT];
