@@ -141,7 +141,7 @@ int mpf3d_compact_init_owner(const int32_t *owner, int slab, const float *prof, 
 int mpf3d_compact_active_count(const uint32_t *head, const uint16_t *idx, int slots, int nx, int ny, int nz,
                                int32_t *nf, void *stream);
 
-/* One fused time step in FP32: APT rebuild (src/gpu_kernels_3d.py:462-486),
+/* One time step in FP32 (three kernels): APT rebuild (src/gpu_kernels_3d.py:462-486),
  * phase update of kernel_update_phasefield_active_3d_switchable (:683-830)
  * and the cooling of kernel_update_temp_3d (:833-838) folded into
  * T = T0z[k] - (Tm_plus_cool - T_melt).  (slots, amax) is (4, 8), (8, 16) or
@@ -154,7 +154,14 @@ int mpf3d_compact_active_count(const uint32_t *head, const uint16_t *idx, int sl
  * Scratch: work_items uint32[cells] (cells handed from the sweep kernel to
  * the general and interface kernels of the step) and work_count uint32[4],
  * zeroed once before the first step; `parity` alternates 0/1 on consecutive
- * steps so no reset is needed in between.  Cells must number fewer than 2^31. */
+ * steps so no reset is needed in between.  Cells must number fewer than 2^31.
+ * Streams: with anisotropy on, the interface kernel runs on a library-owned
+ * second stream of the device, beside the general kernel, forked from and
+ * joined back to `stream` by events; to the caller the step is ordered on
+ * `stream` like one kernel.  The second stream is created by the first such
+ * call made outside a stream capture; a call inside a capture before that
+ * launches both kernels on `stream`.  The same holds for
+ * mpf3d_compact_step_tuned and mpf3d_compact_step_noalloc. */
 int mpf3d_compact_step(const uint32_t *head, const uint16_t *idx, const float *val, uint32_t *head_out,
                        uint16_t *idx_out, float *val_out, int slots, int amax, const double *T0z,
                        double Tm_plus_cool, const float *wij, const float *a2ij, const float *mij,

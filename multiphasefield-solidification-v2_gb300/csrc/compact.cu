@@ -1145,6 +1145,24 @@ dim3 zfast_grid(int nx, int ny, int nz, dim3 b) {
 }
 
 
+// A second stream of one device, on which the interface kernel runs beside
+// the general kernel.  The two read only what the sweep wrote and write
+// disjoint cells; both are latency-bound, so running them side by side
+// fills each other's idle issue slots.  Created on first use outside a
+// stream capture; the fork/join is enqueued under the mutex so that callers
+// on other host threads cannot interleave their event records with it.
+struct SideStream {
+    std::mutex mu;
+    bool ready = false;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
+};
+
+SideStream &side_stream_of(int dev) {
+    static SideStream all[64];
+    return all[dev & 63];
+}
+
 template <int S, int AMAX>
 void launch_step(const In &in, const Out &out, const Mats &M, const Params &P, const Queue &Q, int parity,
                  uint8_t *tile_flags, int32_t *err, cudaStream_t s, const mpf3d_tuning &T) {
@@ -1161,10 +1179,32 @@ void launch_step(const In &in, const Out &out, const Mats &M, const Params &P, c
     int dev = 0, sms = 148;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    general_kernel<S, AMAX><<<sms * T.general_blocks_per_sm, T.general_threads, 0, s>>>(in, out, M, P, Q, parity, err);
-    if (P.use_aniso)
-        interface_kernel<S, AMAX><<<sms * T.iface_blocks_per_sm, T.iface_threads, 0, s>>>(in, out, M, P, Q, parity,
-                                                                                          err);
+    const dim3 g_general(sms * T.general_blocks_per_sm), g_iface(sms * T.iface_blocks_per_sm);
+    if (!P.use_aniso) {
+        general_kernel<S, AMAX><<<g_general, T.general_threads, 0, s>>>(in, out, M, P, Q, parity, err);
+        return;
+    }
+    SideStream &side = side_stream_of(dev);
+    std::lock_guard<std::mutex> lock(side.mu);
+    if (!side.ready) {
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        if (cudaStreamIsCapturing(s, &cs) == cudaSuccess && cs == cudaStreamCaptureStatusNone &&
+            cudaStreamCreateWithFlags(&side.stream, cudaStreamNonBlocking) == cudaSuccess &&
+            cudaEventCreateWithFlags(&side.fork, cudaEventDisableTiming) == cudaSuccess &&
+            cudaEventCreateWithFlags(&side.join, cudaEventDisableTiming) == cudaSuccess)
+            side.ready = true;
+    }
+    if (!side.ready) {  // first call inside a capture: both kernels on the caller's stream
+        general_kernel<S, AMAX><<<g_general, T.general_threads, 0, s>>>(in, out, M, P, Q, parity, err);
+        interface_kernel<S, AMAX><<<g_iface, T.iface_threads, 0, s>>>(in, out, M, P, Q, parity, err);
+        return;
+    }
+    cudaEventRecord(side.fork, s);
+    cudaStreamWaitEvent(side.stream, side.fork, 0);
+    interface_kernel<S, AMAX><<<g_iface, T.iface_threads, 0, side.stream>>>(in, out, M, P, Q, parity, err);
+    general_kernel<S, AMAX><<<g_general, T.general_threads, 0, s>>>(in, out, M, P, Q, parity, err);
+    cudaEventRecord(side.join, side.stream);
+    cudaStreamWaitEvent(s, side.join, 0);  // the caller's stream sees the whole step
 }
 
 bool tuning_ok(const mpf3d_tuning &T) {
