@@ -161,7 +161,14 @@ int mpf3d_compact_active_count(const uint32_t *head, const uint16_t *idx, int sl
  * `stream` like one kernel.  The second stream is created by the first such
  * call made outside a stream capture; a call inside a capture before that
  * launches both kernels on `stream`.  The same holds for
- * mpf3d_compact_step_tuned and mpf3d_compact_step_noalloc. */
+ * mpf3d_compact_step_tuned and mpf3d_compact_step_noalloc; the batched step
+ * (mpf3d_batched_step) runs on `stream` alone. */
+/* Creates the current device's second stream (see "Streams" below) now, so
+ * that steps captured into a CUDA graph later run their general and
+ * interface kernels side by side.  Fails (MPF3D_ERR_CUDA) when `stream` is
+ * being captured.  Optional: the first uncaptured step does the same. */
+int mpf3d_streams_prepare(void *stream);
+
 int mpf3d_compact_step(const uint32_t *head, const uint16_t *idx, const float *val, uint32_t *head_out,
                        uint16_t *idx_out, float *val_out, int slots, int amax, const double *T0z,
                        double Tm_plus_cool, const float *wij, const float *a2ij, const float *mij,

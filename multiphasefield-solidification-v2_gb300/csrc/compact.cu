@@ -1163,6 +1163,45 @@ SideStream &side_stream_of(int dev) {
     return all[dev & 63];
 }
 
+// Creates the side stream and its events once, outside any capture of s.
+bool side_ready(SideStream &side, cudaStream_t s) {
+    if (!side.ready) {
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        if (cudaStreamIsCapturing(s, &cs) == cudaSuccess && cs == cudaStreamCaptureStatusNone &&
+            cudaStreamCreateWithFlags(&side.stream, cudaStreamNonBlocking) == cudaSuccess &&
+            cudaEventCreateWithFlags(&side.fork, cudaEventDisableTiming) == cudaSuccess &&
+            cudaEventCreateWithFlags(&side.join, cudaEventDisableTiming) == cudaSuccess)
+            side.ready = true;
+    }
+    return side.ready;
+}
+
+// general(stream) and interface(stream) launch the two work-list kernels of
+// a step; with `both`, the interface kernel goes to the device's side stream,
+// forked from s after the sweep and joined back before s continues.
+template <class General, class Interface>
+void launch_side_by_side(cudaStream_t s, bool both, General &&general, Interface &&interface) {
+    if (!both) {
+        general(s);
+        return;
+    }
+    int dev = 0;
+    cudaGetDevice(&dev);
+    SideStream &side = side_stream_of(dev);
+    std::lock_guard<std::mutex> lock(side.mu);
+    if (!side_ready(side, s)) {  // first call inside a capture: both kernels on the caller's stream
+        general(s);
+        interface(s);
+        return;
+    }
+    cudaEventRecord(side.fork, s);
+    cudaStreamWaitEvent(side.stream, side.fork, 0);
+    interface(side.stream);
+    general(s);
+    cudaEventRecord(side.join, side.stream);
+    cudaStreamWaitEvent(s, side.join, 0);  // the caller's stream sees the whole step
+}
+
 template <int S, int AMAX>
 void launch_step(const In &in, const Out &out, const Mats &M, const Params &P, const Queue &Q, int parity,
                  uint8_t *tile_flags, int32_t *err, cudaStream_t s, const mpf3d_tuning &T) {
@@ -1180,31 +1219,14 @@ void launch_step(const In &in, const Out &out, const Mats &M, const Params &P, c
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const dim3 g_general(sms * T.general_blocks_per_sm), g_iface(sms * T.iface_blocks_per_sm);
-    if (!P.use_aniso) {
-        general_kernel<S, AMAX><<<g_general, T.general_threads, 0, s>>>(in, out, M, P, Q, parity, err);
-        return;
-    }
-    SideStream &side = side_stream_of(dev);
-    std::lock_guard<std::mutex> lock(side.mu);
-    if (!side.ready) {
-        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
-        if (cudaStreamIsCapturing(s, &cs) == cudaSuccess && cs == cudaStreamCaptureStatusNone &&
-            cudaStreamCreateWithFlags(&side.stream, cudaStreamNonBlocking) == cudaSuccess &&
-            cudaEventCreateWithFlags(&side.fork, cudaEventDisableTiming) == cudaSuccess &&
-            cudaEventCreateWithFlags(&side.join, cudaEventDisableTiming) == cudaSuccess)
-            side.ready = true;
-    }
-    if (!side.ready) {  // first call inside a capture: both kernels on the caller's stream
-        general_kernel<S, AMAX><<<g_general, T.general_threads, 0, s>>>(in, out, M, P, Q, parity, err);
-        interface_kernel<S, AMAX><<<g_iface, T.iface_threads, 0, s>>>(in, out, M, P, Q, parity, err);
-        return;
-    }
-    cudaEventRecord(side.fork, s);
-    cudaStreamWaitEvent(side.stream, side.fork, 0);
-    interface_kernel<S, AMAX><<<g_iface, T.iface_threads, 0, side.stream>>>(in, out, M, P, Q, parity, err);
-    general_kernel<S, AMAX><<<g_general, T.general_threads, 0, s>>>(in, out, M, P, Q, parity, err);
-    cudaEventRecord(side.join, side.stream);
-    cudaStreamWaitEvent(s, side.join, 0);  // the caller's stream sees the whole step
+    launch_side_by_side(
+        s, P.use_aniso,
+        [&](cudaStream_t st) {
+            general_kernel<S, AMAX><<<g_general, T.general_threads, 0, st>>>(in, out, M, P, Q, parity, err);
+        },
+        [&](cudaStream_t st) {
+            interface_kernel<S, AMAX><<<g_iface, T.iface_threads, 0, st>>>(in, out, M, P, Q, parity, err);
+        });
 }
 
 bool tuning_ok(const mpf3d_tuning &T) {
@@ -1329,6 +1351,8 @@ template <int S, int AMAX>
 void launch_batched(const In &in, const Out &out, const Mats &M, const Params &P0, const mpf3d_instance *inst,
                     int n_inst, int n_tiles, const Queue &Q, int parity, int32_t *err, cudaStream_t s) {
     batched_sweep_kernel<S, AMAX><<<n_tiles, dim3(32, 8, 1), 0, s>>>(in, out, P0, inst, n_inst, Q, parity);
+    // one stream: the batch's fixed queue grids already fill the SMs, and the
+    // side-by-side launch of the compact step measured no gain here
     const int sms = sms_of_current_device();
     batched_queue_kernel<S, AMAX, false><<<sms * 8, 256, 0, s>>>(in, out, M, P0, inst, n_inst, Q, parity, err);
     if (P0.use_aniso)
@@ -1336,6 +1360,14 @@ void launch_batched(const In &in, const Out &out, const Mats &M, const Params &P
 }
 
 }  // namespace
+
+extern "C" int mpf3d_streams_prepare(void *stream) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return MPF3D_ERR_CUDA;
+    SideStream &side = side_stream_of(dev);
+    std::lock_guard<std::mutex> lock(side.mu);
+    return side_ready(side, (cudaStream_t)stream) ? MPF3D_OK : MPF3D_ERR_CUDA;
+}
 
 extern "C" int mpf3d_compact_step_tuned(const uint32_t *cnt, const uint16_t *idx, const float *val,
                                         uint32_t *cnt_out, uint16_t *idx_out, float *val_out, int slots, int amax,

@@ -73,6 +73,7 @@ _SIGS = {
     "mpf3d_compact_from_dense": (_I32, [_VP, _I32, _I32, _I32, _I32, _I32, _I32, _VP, _VP, _VP, _VP, _VP]),
     "mpf3d_compact_to_dense": (_I32, [_VP, _VP, _VP, _I32, _I32, _I32, _I32, _I32, _VP, _I32, _VP]),
     "mpf3d_compact_active_count": (_I32, [_VP, _VP, _I32, _I32, _I32, _I32, _VP, _VP]),
+    "mpf3d_streams_prepare": (_I32, [_VP]),
     "mpf3d_compact_step": (_I32, [_VP, _VP, _VP, _VP, _VP, _VP, _I32, _I32, _VP, _F64, _VP, _VP, _VP, _VP,
                                   _I32, _I32, _I32, _I32, ctypes.POINTER(Scalars), _I32, _I32, _I32,
                                   _VP, _VP, _I32, _VP, _VP]),
