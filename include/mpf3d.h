@@ -162,7 +162,9 @@ int mpf3d_compact_active_count(const uint32_t *head, const uint16_t *idx, int sl
  * call made outside a stream capture; a call inside a capture before that
  * launches both kernels on `stream`.  The same holds for
  * mpf3d_compact_step_tuned and mpf3d_compact_step_noalloc; the batched step
- * (mpf3d_batched_step) runs on `stream` alone. */
+ * (mpf3d_batched_step) runs on `stream` alone.  The second stream is shared
+ * by the device's callers: while a capture that holds a step is open, run no
+ * uncaptured step of that device from another host thread. */
 /* Creates the current device's second stream (see "Streams" below) now, so
  * that steps captured into a CUDA graph later run their general and
  * interface kernels side by side.  Fails (MPF3D_ERR_CUDA) when `stream` is

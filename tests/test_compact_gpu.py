@@ -170,3 +170,29 @@ def test_quiet_tile_skipping_changes_nothing(cfg):
     b.step(5)
     a.step(5)
     assert np.array_equal(a.to_dense(), b.to_dense())
+
+
+def test_two_stream_step_replays_from_a_cuda_graph():
+    """The step runs its interface kernel on the library's second stream;
+    after mpf3d_streams_prepare, two steps captured into a CUDA graph (the
+    fork/join is captured with them) and replayed give the eager state bit
+    for bit."""
+    from mpf3d import _lib, inputs
+    case = inputs.voronoi_case(32, 24, 32, 8, 10, seed=5, orientation_seed=2, undercooling=2.0)
+    a, b = make_solver(case), make_solver(case)
+    a.step(2, check=False)
+    dev = torch.device("cuda:0")
+    s = torch.cuda.Stream(dev)
+    s.wait_stream(torch.cuda.current_stream(dev))
+    _lib.check(_lib.lib().mpf3d_streams_prepare(s.cuda_stream), "streams_prepare")
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=s):
+        b.launch_step(1)
+        b.launch_step(2)
+    torch.cuda.current_stream(dev).wait_stream(s)
+    g.replay()
+    torch.cuda.synchronize()
+    b.step_count = 2
+    assert np.array_equal(a.to_dense(), b.to_dense())
+    a.check()
+    b.check()
