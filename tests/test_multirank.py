@@ -70,13 +70,3 @@ def test_single_rank_reductions_are_identity():
     assert bench.max_over_ranks(3.5, 1) == 3.5
     assert bench.sum_over_ranks(2.0, 1) == 2.0
 
-
-def test_committed_traffic_is_read_from_the_step_profile():
-    """bench.py's roofline `traffic` comes from the committed ncu summary of
-    the step kernels; the summary must keep the line it parses, with the
-    per-step DRAM bytes of the three kernels (a few bytes per cell-step)."""
-    import bench
-    t = bench.committed_traffic()
-    assert t is not None
-    cells = 256 ** 3
-    assert 1.0 < t / cells < 20.0
