@@ -69,4 +69,3 @@ def test_single_rank_reductions_are_identity():
     import bench
     assert bench.max_over_ranks(3.5, 1) == 3.5
     assert bench.sum_over_ranks(2.0, 1) == 2.0
-
