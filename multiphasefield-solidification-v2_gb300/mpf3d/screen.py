@@ -26,6 +26,14 @@ def bounded(y: np.ndarray) -> np.ndarray:
     return np.stack([(y[:, 0] - 1.0) / (np.abs(y[:, 0]) + 1.0), y[:, 1] / 45.0], 1)
 
 
+def best_simulated(known: dict, k: int) -> np.ndarray:
+    """The k candidates with the largest simulated value among `known`
+    (candidate -> value; NaN ranks last)."""
+    ids = np.fromiter(known.keys(), dtype=np.int64, count=len(known))
+    vals = np.fromiter(known.values(), dtype=np.float64, count=len(known))
+    return ids[np.argsort(-np.where(np.isfinite(vals), vals, -np.inf), kind="stable")[:k]]
+
+
 def sample_pairs(n: int, seed: int, dT_range=(0.25, 3.0), delta_a_range=(0.0, 1.0)):
     rng = np.random.default_rng(seed)
     q = rng.standard_normal((n, 2, 4))
@@ -137,11 +145,9 @@ def screen(n_candidates=65536, n_train=512, top_k=256, n_audit=256, seed=0, dims
             t_refine += t_new
             for i, v in zip(new.tolist(), bounded(y_new)[:, objective].tolist()):
                 known[i] = v
-    ids = np.fromiter(known.keys(), dtype=np.int64)
-    vals = np.fromiter(known.values(), dtype=np.float64)
-    final_top = ids[np.argsort(-np.where(np.isfinite(vals), vals, -np.inf))[:top_k]]
-    report["final"] = {"rounds": rounds, "recheck": recheck if rounds > 1 else 0, "simulated": int(len(ids)),
-                       "objective_mean": float(np.nanmean(vals[np.isin(ids, final_top)]))}
+    final_top = best_simulated(known, top_k)
+    report["final"] = {"rounds": rounds, "recheck": recheck if rounds > 1 else 0, "simulated": len(known),
+                       "objective_mean": float(np.nanmean([known[i] for i in final_top.tolist()]))}
     report["gpu_seconds"]["refine"] = t_refine
     screened = t_train + t_fit + t_pred + t_chk + t_refine
     report["gpu_seconds"]["screened_total"] = screened
