@@ -294,7 +294,9 @@ def config_dict(args):
                         "(N=65), tanh front, anisotropy+torque on, uniform cooling (config_3d.yaml), "
                         "FP32 compact three-kernel step",
             "grid": list(GRID), "phases": N_GRAINS + 1, "slots": args.slots, "steps": args.steps,
-            "l2": "inputs larger than L2 (compact state > 129 MB per step)",
+            "l2": "inputs larger than L2, no flush: the two state buffers' head arrays alone are "
+                  "2 x 67 MB (> 129 MB L2), plus the stored records; each step reads the previous "
+                  "step's output",
             "parallelism": f"replicas x{args.gpus}" if args.gpus > 1 else "single GPU"}
 
 
