@@ -1,11 +1,14 @@
-// compact.cu -- fused FP32 compact-slot stepper (throughput tier).
+// compact.cu -- FP32 compact-slot stepper (throughput tier).
 //
-// One kernel per time step does what the reference does in three launches
-// (src/gpu_kernels_3d.py:462-486 APT rebuild, :530-680 phase update,
-// :833-838 cooling): it rebuilds each cell's active-phase list from the
-// stored lists of the cell and its 6 face neighbours, evaluates the
-// anisotropic interface, torque and kinetic terms and the pair sums, clips,
-// renormalises and writes only the phases that stay positive.
+// A time step is three kernels that together do what the reference does in
+// three dense launches (src/gpu_kernels_3d.py:462-486 APT rebuild, :530-680
+// phase update, :833-838 cooling): a sweep writes the cells whose
+// neighbourhood holds one phase and queues the rest on work lists; a general
+// kernel and an interface kernel then rebuild each queued cell's
+// active-phase list from the stored lists of the cell and its 6 face
+// neighbours, evaluate the anisotropic interface, torque and kinetic terms
+// and the pair sums, clip, renormalise and write only the phases that stay
+// positive.
 //
 // State layout in HBM (x fastest, so a warp of 32 threads along x reads
 // 32 consecutive entries of each array and an interface -- normal to z --

@@ -215,7 +215,9 @@ def apt_case(ref, name, phi, out_dir=HERE):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default=os.environ.get("MPF3D_REFERENCE_ROOT", "/root/reference"))
+    ap.add_argument("--reference", default=os.environ.get("MPF3D_REFERENCE_ROOT"),
+                    required="MPF3D_REFERENCE_ROOT" not in os.environ,
+                    help="checkout of the reference (or set MPF3D_REFERENCE_ROOT)")
     ap.add_argument("--only", default=None)
     args = ap.parse_args()
     sys.path.insert(0, args.reference)

@@ -56,7 +56,9 @@ def analyse(F, phi0, phi, split, total_time):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default=os.environ.get("MPF3D_REFERENCE_ROOT", "/root/reference"))
+    ap.add_argument("--reference", default=os.environ.get("MPF3D_REFERENCE_ROOT"),
+                    required="MPF3D_REFERENCE_ROOT" not in os.environ,
+                    help="checkout of the reference (or set MPF3D_REFERENCE_ROOT)")
     args = ap.parse_args()
     F = bicrystal_reference.reference_functions(args.reference)
     out = {"groove_keys": np.array(GROOVE_KEYS)}
