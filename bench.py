@@ -290,9 +290,10 @@ def run_reference(args, rank):
 
 
 def config_dict(args):
-    return {"workload": "3D random Voronoi 256^3, 64 grains in the bottom 32 z-layers + liquid "
-                        "(N=65), tanh front, anisotropy+torque on, uniform cooling (config_3d.yaml), "
-                        "FP32 compact three-kernel step",
+    nx, ny, nz = GRID
+    return {"workload": f"3D random Voronoi {nx}x{ny}x{nz}, {N_GRAINS} grains in the bottom {SLAB} z-layers + "
+                        f"liquid (N={N_GRAINS + 1}), tanh front, anisotropy+torque on, uniform cooling "
+                        "(config_3d.yaml), FP32 compact three-kernel step",
             "grid": list(GRID), "phases": N_GRAINS + 1, "slots": args.slots, "steps": args.steps,
             "l2": "inputs larger than L2, no flush: the two state buffers' head arrays alone are "
                   "2 x 67 MB (> 129 MB L2), plus the stored records; each step reads the previous "
@@ -585,25 +586,42 @@ def interface_height(phi_liquid):
     return float(top[ok].double().mean().item()) if bool(ok.any()) else float("nan")
 
 
-def accuracy_run(args, phi0, temp, n111, wij, aij, mij, phys, dev):
-    """Error trajectories against an FP64 run of the reference numerics
-    (dense drop-in kernels, float64 phi, temperature and scalars), all runs in
-    lockstep on the GPU from the same initial state:
+def divergence_study(phi0, temp, n111, wij, aij, mij, phys, dev, steps, slots=16, checkpoints=None,
+                     every_step_until=100, seed=11):
+    """Pointwise FP32-vs-FP64 error trajectories, every run stepped in
+    lockstep on the GPU from the same float32 initial state (so no run starts
+    with a rounding difference):
+      reference (FP64)        -- the dense drop-in kernels with float64 phi,
+                                 temperature and scalars (pinned to the
+                                 oracle at 1e-12);
       fp32_compact            -- the FP32 compact stepper of the bench line;
       f32_reference_numerics  -- the reference's own production typing
-                                 (float32 phi and scalars, float64 arithmetic).
-    At each checkpoint: max|dphi|, entries above 1e-4, mean interface height
-    and grain volume fractions."""
+                                 (float32 phi and scalars, float64 arithmetic);
+      fp64_fp32_storage       -- exact FP64 arithmetic with phi rounded to
+                                 float32 after every step: what storing the
+                                 state in FP32 costs by itself;
+      fp64_noise_1ulp         -- FP64 with a random relative perturbation of
+                                 2^-52 (one float64 ulp) of every value in
+                                 (0, 1) after every step.
+    Per checkpoint and run: max|dphi| against FP64, cells above 1e-4 and
+    1e-6, support flips (a (phase, cell) entry positive in one run and zero
+    in the other), mean interface height and the largest grain
+    volume-fraction difference.  Per run: the first step above 1e-4 and the
+    first step with a support flip (checked every step up to
+    every_step_until, then at the checkpoints)."""
     import torch
     from mpf3d.solver import CompactSolver
     from src import gpu_kernels_3d as K
-    steps = args.accuracy_steps
-    checkpoints = sorted({c for c in (1, 10, 50, 100, 200, 500, 1000, 2000, steps) if c <= steps})
+    if checkpoints is None:
+        checkpoints = (1, 10, 50, 100, 200, 500, 1000, 2000)
+    ck = {c for c in checkpoints if c <= steps} | {steps}
     N, nx, ny, nz = phi0.shape
     cells = nx * ny * nz
     rate = phys.derived()["cooling_rate"]
     W, A, M, U = (torch.from_numpy(np.ascontiguousarray(a)).to(dev) for a in (wij, aij, mij, n111))
     T0 = np.broadcast_to(np.asarray(temp, np.float64), (nx, ny, nz))
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(seed)
 
     class Dense:
         def __init__(self, dtype, f32):
@@ -623,40 +641,74 @@ def accuracy_run(args, phi0, temp, n111, wij, aij, mij, phys, dev):
                                                       nx, ny, nz, N, *self.sc)
             self.p, self.q = self.q, self.p
 
-    r64 = Dense(torch.float64, False)
-    r32 = Dense(torch.float32, True)
-    c = CompactSolver(phi0, temp, n111, wij, aij, mij, phys, slots=args.slots)
+    def noise_1ulp(p):
+        r = torch.rand(p.shape, generator=gen, device=dev, dtype=torch.float32)
+        inner = (p > 0) & (p < 1)
+        p.copy_(torch.where(inner, p * torch.where(r < 0.5, 1.0 - 2.0 ** -52, 1.0 + 2.0 ** -52).double(), p))
 
-    def summary(ref, other):
-        d = (ref - other).abs()
-        vf_r = ref[1:].sum(dim=(1, 2, 3)) / cells
-        vf_o = other[1:].sum(dim=(1, 2, 3)) / cells
-        return {"max_abs_dphi": float(d.max().item()), "entries_above_1e-4": int((d > 1e-4).sum().item()),
-                "interface_height_cells": interface_height(other[0]),
-                "grain_volume_fraction_max_abs_diff": float((vf_r - vf_o).abs().max().item())}
+    ref = Dense(torch.float64, False)
+    runs = {"f32_reference_numerics": Dense(torch.float32, True), "fp64_fp32_storage": Dense(torch.float64, False),
+            "fp64_noise_1ulp": Dense(torch.float64, False)}
+    comp = CompactSolver(phi0, temp, n111, wij, aij, mij, phys, slots=slots)
+    names = ["fp32_compact"] + list(runs)
+    first_above = {k: None for k in names}
+    first_flip = {k: None for k in names}
+
+    def summary(r, o, full):
+        d = (r - o).abs().amax(dim=0)
+        rec = {"max_abs_dphi": float(d.max().item()), "flips": int(((r > 0) != (o > 0)).sum().item())}
+        if full:
+            vf_r = r[1:].sum(dim=(1, 2, 3)) / cells
+            vf_o = o[1:].sum(dim=(1, 2, 3)) / cells
+            rec.update({"cells_above_1e-4": int((d > 1e-4).sum().item()),
+                        "cells_above_1e-6": int((d > 1e-6).sum().item()),
+                        "interface_height_cells": interface_height(o[0]),
+                        "grain_volume_fraction_max_abs_diff": float((vf_r - vf_o).abs().max().item())})
+        return rec
 
     traj = []
     t0 = time.perf_counter()
     for s in range(1, steps + 1):
-        r64.step()
-        r32.step()
-        c.step(1, check=False)
-        if s in checkpoints:
-            ref = r64.p
-            dense32 = c.to_dense(host=False)
-            traj.append({"step": s, "fp64_interface_height_cells": interface_height(ref[0]),
-                         "fp32_compact": summary(ref, dense32.double()),
-                         "f32_reference_numerics": summary(ref, r32.p.double())})
-            del dense32
+        ref.step()
+        for r in runs.values():
+            r.step()
+        runs["fp64_fp32_storage"].p.copy_(runs["fp64_fp32_storage"].p.float())
+        noise_1ulp(runs["fp64_noise_1ulp"].p)
+        comp.step(1, check=False)
+        full = s in ck
+        if not (full or s <= every_step_until):
+            continue
+        rp = ref.p
+        rec = {"step": s}
+        others = {"fp32_compact": comp.to_dense(host=False).double()}
+        for k, r in runs.items():
+            others[k] = r.p.double() if r.p.dtype != torch.float64 else r.p
+        for k in names:
+            rec[k] = summary(rp, others[k], full)
+            if first_above[k] is None and rec[k]["max_abs_dphi"] > 1e-4:
+                first_above[k] = s
+            if first_flip[k] is None and rec[k]["flips"] > 0:
+                first_flip[k] = s
+        del others
+        if full:
+            rec["fp64_interface_height_cells"] = interface_height(rp[0])
+            traj.append(rec)
     torch.cuda.synchronize(dev)
-    c.check()
+    comp.check()
     K.check_errors()
-    out = {"steps": steps, "grid": [nx, ny, nz], "phases": N, "trajectory": traj, "tolerance": 1e-4,
+    out = {"steps": steps, "grid": [nx, ny, nz], "phases": N, "tolerance": 1e-4, "trajectory": traj,
+           "first_step_above_tolerance": first_above, "first_step_with_support_flip": first_flip,
            "seconds": time.perf_counter() - t0,
-           "note": "both float32 paths diverge from FP64 over long horizons at a similar rate"}
-    del r64, r32, c
+           "note": "fp64_fp32_storage is exact FP64 arithmetic on a state rounded to float32 every step; "
+                   "its divergence is what FP32 storage costs by itself"}
+    del ref, runs, comp
     torch.cuda.empty_cache()
     return out
+
+
+def accuracy_run(args, phi0, temp, n111, wij, aij, mij, phys, dev):
+    """The divergence study of the bench workload over --accuracy-steps."""
+    return divergence_study(phi0, temp, n111, wij, aij, mij, phys, dev, args.accuracy_steps, slots=args.slots)
 
 
 def _reduce_scalar(x: float, world: int, op) -> float:
@@ -851,10 +903,15 @@ def main():
     ap.add_argument("--exhaustive", action="store_true", help="c5: also simulate every candidate")
     ap.add_argument("--screen-rounds", type=int, default=2, help="c5: surrogate refit rounds")
     ap.add_argument("--recheck", type=int, default=1024, help="c5: candidates re-simulated per refit round")
+    ap.add_argument("--grains", type=int, default=None,
+                    help="grains of the Voronoi slab (default 64; a crop of the 256^3 workload keeps the grain "
+                         "density with 64 * nx * ny / 256^2)")
     args = ap.parse_args()
-    global GRID
+    global GRID, N_GRAINS
     if args.grid:
         GRID = tuple(args.grid)
+    if args.grains:
+        N_GRAINS = int(args.grains)
     if args.warmup < 3:
         args.warmup = 3
     world = int(os.environ.get("WORLD_SIZE", "1"))
