@@ -164,7 +164,10 @@ int mpf3d_compact_active_count(const uint32_t *head, const uint16_t *idx, int sl
  * mpf3d_compact_step_tuned and mpf3d_compact_step_noalloc; the batched step
  * (mpf3d_batched_step) runs on `stream` alone.  The second stream is shared
  * by the device's callers: while a capture that holds a step is open, run no
- * uncaptured step of that device from another host thread. */
+ * uncaptured step of that device from another host thread.  Because every
+ * caller's interface kernel goes through that one stream, steps of several
+ * solvers issued on independent streams of one device are serialised with
+ * each other. */
 /* Creates the current device's second stream (see "Streams" below) now, so
  * that steps captured into a CUDA graph later run their general and
  * interface kernels side by side.  Fails (MPF3D_ERR_CUDA) when `stream` is
@@ -422,8 +425,10 @@ int mpf3d_f32_to_bf16(const float *x, uint16_t *y, int64_t n, void *stream);
  * array's device address with that device current; make that first call
  * before any stream capture.  All calls share the array and the call clears
  * its counters on `stream` first, so calls that overlap on the GPU (other
- * streams, other host threads) race on it: serialise them.  Other arguments
- * and results are those of mpf3d_compact_step (parity is not needed). */
+ * streams, other host threads) race on it: serialise them.  The device
+ * address is looked up once per device and kept: a cudaDeviceReset after a
+ * call on that device is not supported.  Other arguments and results are
+ * those of mpf3d_compact_step (parity is not needed). */
 int mpf3d_compact_step_noalloc(const uint32_t *head, const uint16_t *idx, const float *val,
                                uint32_t *head_out, uint16_t *idx_out, float *val_out, int slots, int amax,
                                const double *T0z, double Tm_plus_cool, const float *wij, const float *a2ij,

@@ -189,7 +189,13 @@ class CompactSolver:
 
     # -- stepping ---------------------------------------------------------------
     def launch_step(self, step_index: int) -> None:
-        """Enqueue one step (no synchronisation); step_index is 1-based."""
+        """Enqueue one step (no synchronisation); step_index is 1-based.
+
+        The step's temperature (T_melt + step_index * cooling_rate) and its
+        parity are passed by value.  A CUDA graph captured around this call
+        therefore replays the recorded steps as they were: with cooling it
+        is valid for one replay; an isothermal run may replay a graph of an
+        even number of steps repeatedly."""
         src = self.buf[self.cur]
         dst = self.buf[1 - self.cur]
         tmc = self.T_melt + step_index * self.cooling_rate
