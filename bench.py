@@ -152,10 +152,11 @@ def gemm_run(dev, M=65536, N=256, K=256, reps=20):
     W = (torch.randn((N, K), generator=g) * 0.06).to(torch.bfloat16).to(dev)
     b = torch.zeros(N, dtype=torch.float32, device=dev)
     Y = torch.empty((M, N), dtype=torch.bfloat16, device=dev)
+    err = torch.zeros(1, dtype=torch.int32, device=dev)
     st = torch.cuda.current_stream(dev)
     calls = {
         "tc5": lambda: L.mpf3d_gemm_bf16_tc5(M, N, K, X.data_ptr(), K, W.data_ptr(), K, b.data_ptr(), 1, None,
-                                             Y.data_ptr(), N, 1, 0, st.cuda_stream or None),
+                                             Y.data_ptr(), N, 1, 0, err.data_ptr(), st.cuda_stream or None),
         "mma": lambda: L.mpf3d_gemm_bf16_mma(M, N, K, X.data_ptr(), K, 1, W.data_ptr(), 1, K, b.data_ptr(), 1, None,
                                              Y.data_ptr(), N, 1, 0, st.cuda_stream or None),
     }
@@ -180,6 +181,8 @@ def gemm_run(dev, M=65536, N=256, K=256, reps=20):
     except (OSError, KeyError, ValueError):
         peak = FALLBACK_BF16_TFLOPS
         out["peak_bf16_tflops"], out["peak_source"] = peak, "fallback"
+    if int(err.item()):
+        raise RuntimeError("tcgen05 GEMM aborted: " + _lib.describe_dev_error(int(err.item())))
     out["tc5_frac"] = out["tc5_tflops"] / peak
     out["mma_frac"] = out["mma_tflops"] / peak
     return out

@@ -41,6 +41,7 @@ extern "C" {
 #define MPF3D_DEV_BAD_ID 4        /* update met an mf id outside [0, N) */
 #define MPF3D_DEV_SLOT_OVERFLOW 8 /* compact stepper: more phases than slots */
 #define MPF3D_DEV_BAD_INPUT 16    /* compact conversion met a negative/NaN phi */
+#define MPF3D_DEV_GEMM_ABORT 32   /* tcgen05 GEMM: a bounded wait ran out; the CTA's outputs are NaN */
 
 /* compile-time bound on active phases per cell (reference KMAX) */
 #define MPF3D_KMAX 50
@@ -374,18 +375,34 @@ int mpf3d_batched_ray_radii(const uint32_t *head, const uint16_t *idx, const flo
  * B(k,n) = B[k*sbk + n*sbn]; act 0 = none, 1 = SiLU.  Z (nullable) receives
  * the FP32 pre-activation, Y the result (BF16 if y_bf16, else FP32, added to
  * Y when beta = 1), both with row stride ldy.  K-major operands that fit
- * mpf3d_gemm_bf16_tc5 run there, the rest on mpf3d_gemm_bf16_mma. */
+ * mpf3d_gemm_bf16_tc5 run there, the rest on mpf3d_gemm_bf16_mma.  err
+ * (nullable device word) receives MPF3D_DEV_GEMM_ABORT from the tcgen05
+ * kernel. */
 int mpf3d_gemm_bf16(int M, int N, int K, const uint16_t *A, int64_t sam, int64_t sak, const uint16_t *B,
                     int64_t sbk, int64_t sbn, const float *bias, int act, float *Z, void *Y, int ldy,
-                    int y_bf16, int beta, void *stream);
+                    int y_bf16, int beta, int32_t *err, void *stream);
 
 /* The two kernels behind mpf3d_gemm_bf16, callable directly.  _tc5: the
  * tcgen05 kernel (M x N tiles of 128 x N in tensor memory) for K-major A
  * [M][K] (row stride lda) and B given as [N][K] (row stride ldb), K a
  * multiple of 16 up to 256, N up to 256, 16-byte aligned rows; other shapes
- * return MPF3D_ERR_ARG.  _mma: the mma.sync kernel, any strides. */
+ * return MPF3D_ERR_ARG.  _mma: the mma.sync kernel, any strides.
+ * Every mbarrier wait of the tcgen05 kernel is bounded (1 s).  A wait that
+ * runs out stops the CTA's work: the MMAs already issued and the copies in
+ * flight are waited for (again bounded) before the tensor memory is freed,
+ * the CTA's output rows are written as NaN and MPF3D_DEV_GEMM_ABORT is OR-ed
+ * into *err (nullable). */
 int mpf3d_gemm_bf16_tc5(int M, int N, int K, const uint16_t *A, int64_t lda, const uint16_t *B, int64_t ldb,
-                        const float *bias, int act, float *Z, void *Y, int ldy, int y_bf16, int beta, void *stream);
+                        const float *bias, int act, float *Z, void *Y, int ldy, int y_bf16, int beta, int32_t *err,
+                        void *stream);
+
+/* The pipelined tcgen05 kernel of mpf3d_gemm_bf16_tc5 (K a multiple of 64)
+ * with its TMA producer held back, so that no copy and no MMA is ever issued
+ * and every wait of the other roles runs out after wait_ns (at most 0.1 s):
+ * a test of the abort path.  Expected result: MPF3D_DEV_GEMM_ABORT in *err
+ * (required) and NaN in Y.  No reference counterpart. */
+int mpf3d_gemm_bf16_tc5_held(int M, int N, int K, const uint16_t *A, int64_t lda, const uint16_t *B, int64_t ldb,
+                             void *Y, int ldy, int32_t *err, uint64_t wait_ns, void *stream);
 int mpf3d_gemm_bf16_mma(int M, int N, int K, const uint16_t *A, int64_t sam, int64_t sak, const uint16_t *B,
                         int64_t sbk, int64_t sbn, const float *bias, int act, float *Z, void *Y, int ldy,
                         int y_bf16, int beta, void *stream);

@@ -239,7 +239,9 @@ namespace tc5 {
 constexpr int TM = 128;
 constexpr int MAX_N = 256;
 constexpr int MAX_K = 256;
-constexpr uint32_t POLL_LIMIT = 1u << 24;
+// bound of every mbarrier wait (nanoseconds of %globaltimer); a wait that
+// runs out aborts the CTA's work and reports MPF3D_DEV_GEMM_ABORT
+constexpr uint64_t WAIT_LIMIT_NS = 1000000000ull;
 
 __device__ __forceinline__ uint32_t smem_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -256,8 +258,17 @@ __host__ __device__ __forceinline__ uint32_t instr_desc(int m, int n) {
     return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
 }
 
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
-    for (uint32_t it = 0; it < POLL_LIMIT; ++it) {
+__device__ __forceinline__ uint64_t global_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// waits for the phase `parity` of an mbarrier to complete, for at most
+// limit_ns; false if it did not
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, uint64_t limit_ns = WAIT_LIMIT_NS) {
+    const uint64_t t0 = global_ns();
+    while (true) {
         uint32_t ok;
         asm volatile(
             "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.b32 %0, 1, 0, p;\n}\n"
@@ -265,8 +276,8 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
             : "r"(bar), "r"(parity)
             : "memory");
         if (ok) return true;
+        if (global_ns() - t0 > limit_ns) return false;
     }
-    return false;
 }
 
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
@@ -316,7 +327,8 @@ __device__ __forceinline__ void stage(uint8_t *dst, const uint16_t *__restrict__
 __global__ void __launch_bounds__(128) gemm_kernel(int M, int N, int K, const uint16_t *__restrict__ A, int64_t lda,
                                                    const uint16_t *__restrict__ B, int64_t ldb,
                                                    const float *__restrict__ bias, int act, float *__restrict__ Z,
-                                                   void *__restrict__ Y, int ldy, int y_bf16, int beta) {
+                                                   void *__restrict__ Y, int ldy, int y_bf16, int beta,
+                                                   int32_t *__restrict__ err) {
     extern __shared__ __align__(1024) uint8_t smem[];
     const int n_mma = (N + 15) & ~15;
     uint8_t *sA = smem;
@@ -438,9 +450,12 @@ __global__ void __launch_bounds__(128) gemm_kernel(int M, int N, int K, const ui
             break;
         }
     }
-    if (!ok) mbar_wait(bar_a, (uint32_t)(it & 1));  // let an overdue MMA drain before the memory is freed
-    __syncthreads();
-    if (warp == 0) {
+    // an overdue MMA must finish before its memory is freed: if its commit
+    // never arrives, the tensor memory is left allocated rather than freed
+    // under a running MMA
+    const bool drained = __syncthreads_and(ok || mbar_wait(bar_a, (uint32_t)(it & 1))) != 0;
+    if (!ok && threadIdx.x == 0 && err) atomicOr(err, MPF3D_DEV_GEMM_ABORT);
+    if (warp == 0 && drained) {
         asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
         tmem = *tslot;
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(ncols) : "memory");
@@ -512,7 +527,8 @@ __global__ void __launch_bounds__(320, 1) gemm_kernel(const __grid_constant__ CU
                                                       const __grid_constant__ CUtensorMap map_w, int M, int N, int K,
                                                       const float *__restrict__ bias, int act,
                                                       float *__restrict__ Z, void *__restrict__ Y, int ldy,
-                                                      int y_bf16, int beta) {
+                                                      int y_bf16, int beta, int32_t *__restrict__ err,
+                                                      uint64_t wait_ns, int hold_producer) {
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     // 1024-byte alignment for the swizzled tiles
     uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
@@ -522,14 +538,16 @@ __global__ void __launch_bounds__(320, 1) gemm_kernel(const __grid_constant__ CU
     uint8_t *sW = smem;
     uint8_t *sA = sW + KA * w_atom_bytes;
     uint64_t *bars = reinterpret_cast<uint64_t *>(sA + STAGES * A_STAGE_BYTES);
-    // bars: full[STAGES], empty[STAGES], acc_full[2], acc_empty[2], w_full
-    uint32_t *tslot = reinterpret_cast<uint32_t *>(bars + 2 * STAGES + 5);
+    // bars: full[STAGES], empty[STAGES], acc_full[2], acc_empty[2], w_full, drain
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(bars + 2 * STAGES + 6);
     int *abort_flag = reinterpret_cast<int *>(tslot + 1);
+    int *undrained = abort_flag + 1;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t buf_cols = n_mma <= 32 ? 32u : (n_mma <= 64 ? 64u : (n_mma <= 128 ? 128u : 256u));
     const int tiles = (M + TM - 1) / TM;
     auto bar = [&](int i) { return smem_addr(bars + i); };
-    const int FULL = 0, EMPTY = STAGES, ACC_FULL = 2 * STAGES, ACC_EMPTY = 2 * STAGES + 2, W_FULL = 2 * STAGES + 4;
+    const int FULL = 0, EMPTY = STAGES, ACC_FULL = 2 * STAGES, ACC_EMPTY = 2 * STAGES + 2, W_FULL = 2 * STAGES + 4,
+              DRAIN = 2 * STAGES + 5;
 
     if (threadIdx.x == 0) {
         for (int i = 0; i < STAGES; ++i) {
@@ -541,8 +559,10 @@ __global__ void __launch_bounds__(320, 1) gemm_kernel(const __grid_constant__ CU
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 8;\n" ::"r"(bar(ACC_EMPTY + b)) : "memory");
         }
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar(W_FULL)) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar(DRAIN)) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
         *abort_flag = 0;
+        *undrained = 0;
     }
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_addr(tslot)),
@@ -557,13 +577,15 @@ __global__ void __launch_bounds__(320, 1) gemm_kernel(const __grid_constant__ CU
     volatile int *abort_v = abort_flag;
     auto wait = [&](int i, uint32_t parity) -> bool {
         if (*abort_v) return false;
-        if (mbar_wait(bar(i), parity)) return true;
+        if (mbar_wait(bar(i), parity, wait_ns)) return true;
         *abort_v = 1;
         return false;
     };
 
     if (warp == 0) {
-        if (lane == 0) {
+        // hold_producer (a test of the abort path) keeps the producer from
+        // issuing anything: every wait of the other roles then runs out
+        if (lane == 0 && !hold_producer) {
             // weights once
             arrive_expect(bar(W_FULL), (uint32_t)KA * w_atom_bytes);
             for (int j = 0; j < KA; ++j) tma_load(smem_addr(sW + j * w_atom_bytes), &map_w, j * ATOM_K, 0, bar(W_FULL));
@@ -580,14 +602,17 @@ __global__ void __launch_bounds__(320, 1) gemm_kernel(const __grid_constant__ CU
             }
             // every copy issued must land before the CTA can go away
             if (*abort_v) {
+                bool landed = true;
                 for (uint32_t q = issued > STAGES ? issued - STAGES : 0; q < issued; ++q)
-                    mbar_wait(bar(FULL + q % STAGES), (q / STAGES) & 1u);
-                mbar_wait(bar(W_FULL), 0);
+                    landed = mbar_wait(bar(FULL + q % STAGES), (q / STAGES) & 1u, wait_ns) && landed;
+                landed = mbar_wait(bar(W_FULL), 0, wait_ns) && landed;
+                if (!landed) atomicExch(undrained, 1);
             }
         }
     } else if (warp == 1) {
         if (lane == 0) {
             const uint32_t idesc = instr_desc(TM, n_mma);
+            bool issued = false;
             if (wait(W_FULL, 0)) {
                 uint32_t it = 0, t_local = 0;
                 for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x, ++t_local) {
@@ -609,11 +634,19 @@ __global__ void __launch_bounds__(320, 1) gemm_kernel(const __grid_constant__ CU
                         for (int ks = 0; ks < ATOM_K / 16; ++ks)
                             umma(d, sw128_desc(a_base + 32u * ks), sw128_desc(w_base + 32u * ks), idesc,
                                  (j > 0 || ks > 0) ? 1u : 0u);
+                        issued = true;
                         commit(bar(EMPTY + s));  // the stage is free once these MMAs are done
                     }
                     if (!ok) break;
                     commit(bar(ACC_FULL + b));
                 }
+            }
+            if (*abort_v && issued) {
+                // the MMAs issued before the abort must finish before the
+                // tensor memory is freed and the CTA leaves: one more commit
+                // arrives once all of them are done
+                commit(bar(DRAIN));
+                if (!mbar_wait(bar(DRAIN), 0, wait_ns)) atomicExch(undrained, 1);
             }
         }
     } else {
@@ -693,6 +726,7 @@ __global__ void __launch_bounds__(320, 1) gemm_kernel(const __grid_constant__ CU
     __syncthreads();
     if (*abort_v && threadIdx.x == 0) {
         // an aborted run: the outputs of this CTA's tiles are unreliable
+        if (err) atomicOr(err, MPF3D_DEV_GEMM_ABORT);
         for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x)
             for (int r = 0; r < TM && tile * TM + r < M; ++r) {
                 const int64_t o = (int64_t)(tile * TM + r) * ldy;
@@ -702,7 +736,8 @@ __global__ void __launch_bounds__(320, 1) gemm_kernel(const __grid_constant__ CU
                 }
             }
     }
-    if (warp == 0) {
+    // tensor memory that an undrained MMA may still write is left allocated
+    if (warp == 0 && !*(volatile int *)undrained) {
         asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(2 * buf_cols)
                      : "memory");
@@ -771,27 +806,36 @@ static bool make_map(CUtensorMap *map, const uint16_t *base, int rows, int K, in
               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
+// the pipelined kernel (K a multiple of 64); hold_producer != 0 only in the
+// abort-path test.  Returns 1 when no tensor map could be made.
+static int launch_tc5_tma(int M, int N, int K, const uint16_t *A, int64_t lda, const uint16_t *B, int64_t ldb,
+                          const float *bias, int act, float *Z, void *Y, int ldy, int y_bf16, int beta, int32_t *err,
+                          uint64_t wait_ns, int hold_producer, cudaStream_t stream) {
+    using namespace mpf3d::mlp;
+    CUtensorMap mx, mw;
+    const int n_mma = (N + 15) & ~15;
+    if (!make_map(&mx, A, M, K, lda, tc5::TM) || !make_map(&mw, B, N, K, ldb, n_mma)) return 1;
+    const size_t bytes = tc5::tma::smem_bytes(N, K);
+    if (cudaFuncSetAttribute(tc5::tma::gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) !=
+        cudaSuccess)
+        return MPF3D_ERR_CUDA;
+    const int tiles = (M + tc5::TM - 1) / tc5::TM;
+    const int grid = tiles < sms_of_device() ? tiles : sms_of_device();
+    tc5::tma::gemm_kernel<<<grid, 320, bytes, stream>>>(mx, mw, M, N, K, bias, act, Z, Y, ldy, y_bf16, beta, err,
+                                                        wait_ns, hold_producer);
+    return cudaGetLastError() == cudaSuccess ? MPF3D_OK : MPF3D_ERR_CUDA;
+}
+
 extern "C" int mpf3d_gemm_bf16_tc5(int M, int N, int K, const uint16_t *A, int64_t lda, const uint16_t *B,
                                    int64_t ldb, const float *bias, int act, float *Z, void *Y, int ldy, int y_bf16,
-                                   int beta, void *stream) {
+                                   int beta, int32_t *err, void *stream) {
     using namespace mpf3d::mlp;
     if (!A || !B || !Y || ldy < N || (act != 0 && act != 1) || !tc5_shape_ok(M, N, K, A, lda, B, ldb))
         return MPF3D_ERR_ARG;
     if (K % tc5::tma::ATOM_K == 0) {
-        // the pipelined kernel: operands arrive by TMA
-        CUtensorMap mx, mw;
-        const int n_mma = (N + 15) & ~15;
-        if (make_map(&mx, A, M, K, lda, tc5::TM) && make_map(&mw, B, N, K, ldb, n_mma)) {
-            const size_t bytes = tc5::tma::smem_bytes(N, K);
-            if (cudaFuncSetAttribute(tc5::tma::gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) !=
-                cudaSuccess)
-                return MPF3D_ERR_CUDA;
-            const int tiles = (M + tc5::TM - 1) / tc5::TM;
-            const int grid = tiles < sms_of_device() ? tiles : sms_of_device();
-            tc5::tma::gemm_kernel<<<grid, 320, bytes, (cudaStream_t)stream>>>(mx, mw, M, N, K, bias, act, Z, Y, ldy,
-                                                                             y_bf16, beta);
-            return cudaGetLastError() == cudaSuccess ? MPF3D_OK : MPF3D_ERR_CUDA;
-        }
+        const int rc = launch_tc5_tma(M, N, K, A, lda, B, ldb, bias, act, Z, Y, ldy, y_bf16, beta, err,
+                                      tc5::WAIT_LIMIT_NS, 0, (cudaStream_t)stream);
+        if (rc != 1) return rc;  // 1: no tensor map, use the register-staged form
     }
     const size_t bytes = tc5::smem_bytes(N, K);
     if (cudaFuncSetAttribute(tc5::gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) !=
@@ -801,8 +845,19 @@ extern "C" int mpf3d_gemm_bf16_tc5(int M, int N, int K, const uint16_t *A, int64
     const int per_sm = bytes > 114 * 1024 ? 1 : 2;
     const int grid = tiles < sms_of_device() * per_sm ? tiles : sms_of_device() * per_sm;
     tc5::gemm_kernel<<<grid, 128, bytes, (cudaStream_t)stream>>>(M, N, K, A, lda, B, ldb, bias, act, Z, Y, ldy,
-                                                                 y_bf16, beta);
+                                                                 y_bf16, beta, err);
     return cudaGetLastError() == cudaSuccess ? MPF3D_OK : MPF3D_ERR_CUDA;
+}
+
+extern "C" int mpf3d_gemm_bf16_tc5_held(int M, int N, int K, const uint16_t *A, int64_t lda, const uint16_t *B,
+                                        int64_t ldb, void *Y, int ldy, int32_t *err, uint64_t wait_ns, void *stream) {
+    using namespace mpf3d::mlp;
+    if (!A || !B || !Y || !err || ldy < N || K % tc5::tma::ATOM_K != 0 || wait_ns == 0 || wait_ns > 100000000ull ||
+        !tc5_shape_ok(M, N, K, A, lda, B, ldb))
+        return MPF3D_ERR_ARG;
+    const int rc = launch_tc5_tma(M, N, K, A, lda, B, ldb, nullptr, 0, nullptr, Y, ldy, 0, 0, err, wait_ns, 1,
+                                  (cudaStream_t)stream);
+    return rc == 1 ? MPF3D_ERR_CUDA : rc;
 }
 
 extern "C" int mpf3d_gemm_bf16_mma(int M, int N, int K, const uint16_t *A, int64_t sam, int64_t sak,
@@ -818,11 +873,11 @@ extern "C" int mpf3d_gemm_bf16_mma(int M, int N, int K, const uint16_t *A, int64
 
 extern "C" int mpf3d_gemm_bf16(int M, int N, int K, const uint16_t *A, int64_t sam, int64_t sak, const uint16_t *B,
                                int64_t sbk, int64_t sbn, const float *bias, int act, float *Z, void *Y, int ldy,
-                               int y_bf16, int beta, void *stream) {
+                               int y_bf16, int beta, int32_t *err, void *stream) {
     // K-major operands (the forward pass X W^T) go to the tcgen05 kernel;
     // transposed ones (the gradients) to the mma.sync kernel
     if (sak == 1 && sbk == 1 && tc5_shape_ok(M, N, K, A, sam, B, sbn))
-        return mpf3d_gemm_bf16_tc5(M, N, K, A, sam, B, sbn, bias, act, Z, Y, ldy, y_bf16, beta, stream);
+        return mpf3d_gemm_bf16_tc5(M, N, K, A, sam, B, sbn, bias, act, Z, Y, ldy, y_bf16, beta, err, stream);
     return mpf3d_gemm_bf16_mma(M, N, K, A, sam, sak, B, sbk, sbn, bias, act, Z, Y, ldy, y_bf16, beta, stream);
 }
 

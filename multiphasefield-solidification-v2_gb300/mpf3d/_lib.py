@@ -19,7 +19,8 @@ DEV_BITS = {1: "unchecked APT needed more rows than mf has (MPF3D_DEV_MF_DEPTH)"
             2: "update met nf > KMAX (MPF3D_DEV_NF_GT_KMAX)",
             4: "update met an mf id outside [0, N) (MPF3D_DEV_BAD_ID)",
             8: "compact stepper: more phases than slots (MPF3D_DEV_SLOT_OVERFLOW)",
-            16: "compact conversion met a negative or NaN phi (MPF3D_DEV_BAD_INPUT)"}
+            16: "compact conversion met a negative or NaN phi (MPF3D_DEV_BAD_INPUT)",
+            32: "tcgen05 GEMM: a bounded wait ran out, outputs written as NaN (MPF3D_DEV_GEMM_ABORT)"}
 
 _VP = ctypes.c_void_p
 _I32 = ctypes.c_int
@@ -87,11 +88,13 @@ _SIGS = {
     "mpf3d_batched_gb_rows": (_I32, [_VP, _VP, _VP, _I32, _VP, _I32, ctypes.c_uint32, _VP, _VP, _VP]),
     "mpf3d_compact_init_owner": (_I32, [_VP, _I32, _VP, _I32, _I32, _I32, _I32, _VP, _VP, _VP, _VP]),
     "mpf3d_gemm_bf16": (_I32, [_I32, _I32, _I32, _VP, _I64, _I64, _VP, _I64, _I64, _VP, _I32, _VP, _VP, _I32,
-                               _I32, _I32, _VP]),
+                               _I32, _I32, _VP, _VP]),
     "mpf3d_gemm_bf16_mma": (_I32, [_I32, _I32, _I32, _VP, _I64, _I64, _VP, _I64, _I64, _VP, _I32, _VP, _VP, _I32,
                                _I32, _I32, _VP]),
     "mpf3d_gemm_bf16_tc5": (_I32, [_I32, _I32, _I32, _VP, _I64, _VP, _I64, _VP, _I32, _VP, _VP, _I32, _I32, _I32,
-                                   _VP]),
+                                   _VP, _VP]),
+    "mpf3d_gemm_bf16_tc5_held": (_I32, [_I32, _I32, _I32, _VP, _I64, _VP, _I64, _VP, _I32, _VP, ctypes.c_uint64,
+                                        _VP]),
     "mpf3d_act_backward": (_I32, [_VP, _VP, _I32, _I64, _VP, _VP, _VP]),
     "mpf3d_colsum": (_I32, [_VP, _I32, _I32, _I32, _VP, _VP]),
     "mpf3d_mse": (_I32, [_VP, _I32, _VP, _I32, _I32, _VP, _VP, _VP, _VP]),

@@ -148,6 +148,8 @@ class Surrogate:
         self.mean = np.zeros(OUT, np.float32)
         self.std = np.ones(OUT, np.float32)
         self.loss_w = t.ones(OUT, dtype=t.float32, device=self.device)
+        # device error word of the tcgen05 GEMM (MPF3D_DEV_GEMM_ABORT), read by check()
+        self.gemm_err = t.zeros(1, dtype=t.int32, device=self.device)
 
     # -- helpers -------------------------------------------------------------------
     def _s(self):
@@ -166,7 +168,7 @@ class Surrogate:
         rc = _lib.lib().mpf3d_gemm_bf16(M, N, K, A.data_ptr(), sam, sak, B.data_ptr(), sbk, sbn,
                                         bias.data_ptr() if bias is not None else None, act,
                                         Z.data_ptr() if Z is not None else None, Y.data_ptr(), ldy, int(y_bf16),
-                                        beta, self._s())
+                                        beta, self.gemm_err.data_ptr(), self._s())
         _lib.check(rc, "gemm_bf16")
 
     def prepare(self, X: np.ndarray):
@@ -281,7 +283,15 @@ class Surrogate:
                 self.adam(lr=lr * (0.5 * (1 + np.cos(np.pi * ep / epochs))))
                 ep_loss += float(loss.item()) * len(idx) / n
             hist.append(ep_loss)
+        self.check()
         return hist
+
+    def check(self) -> None:
+        """Raise if a tcgen05 GEMM of this network aborted on a wait that ran out."""
+        v = int(self.gemm_err.item())
+        if v:
+            self.gemm_err.zero_()
+            raise RuntimeError("surrogate GEMM device error: " + _lib.describe_dev_error(v))
 
     def predict(self, q1, q2, undercooling, delta_a, chunk: int = 65536) -> np.ndarray:
         """[M, 2] predictions in target units."""
@@ -290,6 +300,7 @@ class Surrogate:
         for s in range(0, len(X), chunk):
             x16 = self.prepare(X[s:s + chunk])
             outs.append(self.forward(x16).cpu().numpy())
+        self.check()
         return np.concatenate(outs) * self.std + self.mean
 
     def bf16_weights(self):

@@ -40,7 +40,7 @@ def test_gemm_matches_float64(M, N, K, transA, transB):
     Y = torch.empty((M, N), dtype=torch.float32, device=dev)
     Z = torch.empty((M, N), dtype=torch.float32, device=dev)
     rc = _lib.lib().mpf3d_gemm_bf16(M, N, K, tA.data_ptr(), sam, sak, tB.data_ptr(), sbk, sbn, tb.data_ptr(), 1,
-                                    Z.data_ptr(), Y.data_ptr(), N, 0, 0, None)
+                                    Z.data_ptr(), Y.data_ptr(), N, 0, 0, None, None)
     assert rc == 0
     ref_z = bf16_round(A) @ bf16_round(B) + bias
     ref_y = ref_z / (1.0 + np.exp(-ref_z))
@@ -71,9 +71,11 @@ def test_tcgen05_gemm_matches_float64(M, N, K, act, y_bf16):
     ydt = torch.int16 if y_bf16 else torch.float32
     Z = torch.full((M, N), float("nan"), dtype=torch.float32, device=dev)
     Y = torch.zeros((M, N), dtype=ydt, device=dev)
+    err = torch.zeros(1, dtype=torch.int32, device=dev)
     rc = _lib.lib().mpf3d_gemm_bf16_tc5(M, N, K, tX.data_ptr(), K, tW.data_ptr(), K, tb.data_ptr(), act,
-                                        Z.data_ptr(), Y.data_ptr(), N, y_bf16, 0, None)
+                                        Z.data_ptr(), Y.data_ptr(), N, y_bf16, 0, err.data_ptr(), None)
     assert rc == 0
+    assert int(err.item()) == 0
     ref_z = bf16_round(X) @ bf16_round(W).T + bias
     got_z = Z.cpu().numpy()
     scale = np.abs(ref_z).max()
@@ -97,9 +99,42 @@ def test_tcgen05_rejects_shapes_it_does_not_cover():
     from mpf3d import _lib
     L = _lib.lib()
     p = 0x10000
-    assert L.mpf3d_gemm_bf16_tc5(64, 300, 64, p, 64, p, 64, None, 0, None, p, 300, 0, 0, None) == -1  # N > 256
-    assert L.mpf3d_gemm_bf16_tc5(64, 64, 24, p, 24, p, 24, None, 0, None, p, 64, 0, 0, None) == -1    # K % 16
-    assert L.mpf3d_gemm_bf16_tc5(64, 64, 512, p, 512, p, 512, None, 0, None, p, 64, 0, 0, None) == -1  # K > 256
+    assert L.mpf3d_gemm_bf16_tc5(64, 300, 64, p, 64, p, 64, None, 0, None, p, 300, 0, 0, None, None) == -1  # N > 256
+    assert L.mpf3d_gemm_bf16_tc5(64, 64, 24, p, 24, p, 24, None, 0, None, p, 64, 0, 0, None, None) == -1    # K % 16
+    assert L.mpf3d_gemm_bf16_tc5(64, 64, 512, p, 512, p, 512, None, 0, None, p, 64, 0, 0, None, None) == -1  # K > 256
+
+
+def test_tcgen05_abort_path_reports_and_frees():
+    """The pipelined kernel with its TMA producer held back: no copy and no
+    MMA is ever issued, so every bounded wait of the MMA and epilogue roles
+    runs out (after 20 ms).  The kernel must report MPF3D_DEV_GEMM_ABORT,
+    write NaN, free its tensor memory and leave the context usable: an
+    ordinary GEMM right after it gives the right answer twice."""
+    from mpf3d import _lib
+    L = _lib.lib()
+    M, N, K = 512, 128, 64
+    rng = np.random.default_rng(3)
+    X = rng.standard_normal((M, K)).astype(np.float32)
+    W = rng.standard_normal((N, K)).astype(np.float32)
+    dev = torch.device("cuda:0")
+    tX = torch.from_numpy(to_bf16_bits(X)).to(dev)
+    tW = torch.from_numpy(to_bf16_bits(W)).to(dev)
+    Y = torch.zeros((M, N), dtype=torch.float32, device=dev)
+    err = torch.zeros(1, dtype=torch.int32, device=dev)
+    assert L.mpf3d_gemm_bf16_tc5_held(M, N, K, tX.data_ptr(), K, tW.data_ptr(), K, Y.data_ptr(), N,
+                                      err.data_ptr(), 20_000_000, None) == 0
+    torch.cuda.synchronize()
+    assert int(err.item()) & 32
+    assert torch.isnan(Y).all()
+    ref = bf16_round(X) @ bf16_round(W).T
+    for _ in range(2):
+        err.zero_()
+        Y.zero_()
+        assert L.mpf3d_gemm_bf16_tc5(M, N, K, tX.data_ptr(), K, tW.data_ptr(), K, None, 0, None, Y.data_ptr(), N, 0,
+                                     0, err.data_ptr(), None) == 0
+        torch.cuda.synchronize()
+        assert int(err.item()) == 0
+        assert np.abs(Y.cpu().numpy() - ref).max() <= 1e-5 * np.abs(ref).max() * np.sqrt(K)
 
 
 def cpu_forward_backward(layers, X, target, w):
