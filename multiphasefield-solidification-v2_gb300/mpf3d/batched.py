@@ -338,8 +338,15 @@ class BatchedBicrystals:
                 v2[i] = np.polyfit(times[ok], A2[i, ok], 1)[0] / ((nx - split) * ny)
         with np.errstate(invalid="ignore", divide="ignore"):
             ratio = v1 / v2
+        # why a ratio is not finite: 1 = fewer than two samples before a front
+        # came within 6 cells of the top (fast growth in a short box), 2 =
+        # grain 2 does not grow (zero fitted velocity)
+        status = np.zeros(self.n, np.int32)
+        status[~np.isfinite(v1) | ~np.isfinite(v2)] = 1
+        status[(status == 0) & (v2 == 0.0)] = 2
+        status[(status == 0) & ~np.isfinite(ratio)] = 3
         return {"v1": v1, "v2": v2, "velocity_ratio": ratio, "gb_angle_deg": self.gb_inclination(),
-                "times": times, "h1": H1, "h2": H2, "V1": A1, "V2": A2}
+                "times": times, "h1": H1, "h2": H2, "V1": A1, "V2": A2, "ratio_status": status}
 
 
 def sample_batch(n: int, seed: int = 0, sizes_xy=(64, 96, 128), sizes_z=(64, 96), dT_range=(0.25, 3.0),

@@ -41,20 +41,29 @@ def sample_pairs(n: int, seed: int, dT_range=(0.25, 3.0), delta_a_range=(0.0, 1.
     return q[:, 0], q[:, 1], rng.uniform(*dT_range, n), rng.uniform(*delta_a_range, n)
 
 
+def candidate_dims(n: int, seed: int, sizes_xy=(64, 96, 128), sizes_z=(64, 96)):
+    """Per-candidate grid sizes drawn uniformly from sizes_xy^2 x sizes_z (the
+    batched-bicrystal workload's instance sizes)."""
+    rng = np.random.default_rng(seed)
+    return [(int(rng.choice(sizes_xy)), int(rng.choice(sizes_xy)), int(rng.choice(sizes_z))) for _ in range(n)]
+
+
 def simulate(q1, q2, dT, da, dims=(32, 32, 64), steps=300, sample_every=10, batch=4096, base_height=16.0,
              device="cuda:0"):
     """Velocity ratio and grain-boundary inclination of every pair, simulated
-    in batches of `batch` instances; returns ([n, 2] targets, GPU seconds)."""
+    in batches of `batch` instances; dims is one (nx, ny, nz) for every pair or
+    a list with one per pair.  Returns ([n, 2] targets, GPU seconds)."""
     import torch
 
     n = len(q1)
+    per_pair = isinstance(dims, list)
     out = np.full((n, 2), np.nan)
     t0 = time.perf_counter()
     for s in range(0, n, batch):
         e = min(n, s + batch)
         q = np.stack([q1[s:e], q2[s:e]], 1)
-        b = BatchedBicrystals([dims] * (e - s), q, dT[s:e], da[s:e], base_height=base_height, slots=4,
-                              device=device)
+        b = BatchedBicrystals(dims[s:e] if per_pair else [dims] * (e - s), q, dT[s:e], da[s:e],
+                              base_height=base_height, slots=4, device=device)
         b.capture(sample_every if sample_every % 2 == 0 else 2 * sample_every)
         r = b.run(steps, sample_every=sample_every, graph_steps=0)
         out[s:e, 0] = r["velocity_ratio"]
@@ -65,7 +74,8 @@ def simulate(q1, q2, dT, da, dims=(32, 32, 64), steps=300, sample_every=10, batc
 
 
 def screen(n_candidates=65536, n_train=512, top_k=256, n_audit=256, seed=0, dims=(32, 32, 64), steps=300,
-           epochs=300, objective=0, exhaustive=False, rounds=1, recheck=1024, device="cuda:0"):
+           epochs=300, objective=0, exhaustive=False, rounds=1, recheck=1024, device="cuda:0", batch=4096,
+           sample_every=10):
     """Rank n_candidates pairs by the surrogate's prediction of target
     `objective` (0 velocity ratio, 1 grain-boundary inclination; larger is
     better) and check it by re-simulation.  Errors and objective values are
@@ -76,14 +86,25 @@ def screen(n_candidates=65536, n_train=512, top_k=256, n_audit=256, seed=0, dims
     the audit sample), and its top `recheck` candidates that have not been
     simulated yet are simulated.  The answer (`final`) is then the top_k of
     all simulated candidates by their simulated value.  Every GPU second of
-    the refinement counts in `screened_total`.  Returns a report dict."""
+    the refinement counts in `screened_total`.  dims is one grid for every
+    candidate, or "ragged": per-candidate sizes from candidate_dims (the
+    batched-bicrystal workload's {64,96,128}^2 x {64,96}).  Returns a report
+    dict."""
     import torch
 
     q1, q2, dT, da = sample_pairs(n_candidates, seed)
+    dims_all = candidate_dims(n_candidates, seed + 7) if dims == "ragged" else None
+
+    def dims_of(idx):
+        return [dims_all[i] for i in np.asarray(idx).tolist()] if dims_all is not None else dims
+
+    def sim(idx):
+        return simulate(q1[idx], q2[idx], dT[idx], da[idx], dims_of(idx), steps, sample_every=sample_every,
+                        batch=batch, device=device)
+
     rng = np.random.default_rng(seed + 1)
     train_idx = rng.choice(n_candidates, n_train, replace=False)
-    y_train, t_train = simulate(q1[train_idx], q2[train_idx], dT[train_idx], da[train_idx], dims, steps,
-                                device=device)
+    y_train, t_train = sim(train_idx)
     t0 = time.perf_counter()
     s = Surrogate(seed=seed, device=device)
     hist = s.fit(q1[train_idx], q2[train_idx], dT[train_idx], da[train_idx], bounded(y_train), epochs=epochs,
@@ -98,7 +119,7 @@ def screen(n_candidates=65536, n_train=512, top_k=256, n_audit=256, seed=0, dims
     top = order[:top_k]
     audit = rng.choice(n_candidates, n_audit, replace=False)
     chk_idx = np.concatenate([top, audit])
-    y_chk, t_chk = simulate(q1[chk_idx], q2[chk_idx], dT[chk_idx], da[chk_idx], dims, steps, device=device)
+    y_chk, t_chk = sim(chk_idx)
     y_chk = bounded(y_chk)
     p_chk = pred[chk_idx]
 
@@ -111,7 +132,7 @@ def screen(n_candidates=65536, n_train=512, top_k=256, n_audit=256, seed=0, dims
     y_top, y_aud = y_chk[:top_k, objective], y_chk[top_k:, objective]
     report = {
         "candidates": n_candidates, "train": n_train, "top_k": top_k, "audit": n_audit,
-        "dims": list(dims), "steps": steps, "objective": ["velocity_ratio", "gb_inclination_deg"][objective],
+        "dims": dims if isinstance(dims, str) else list(dims), "steps": steps, "objective": ["velocity_ratio", "gb_inclination_deg"][objective],
         "train_loss_first_last": [hist[0], hist[-1]],
         "surrogate_error_top": err(p_chk[:top_k], y_chk[:top_k]),
         "surrogate_error_audit": err(p_chk[top_k:], y_chk[top_k:]),
@@ -141,7 +162,7 @@ def screen(n_candidates=65536, n_train=512, top_k=256, n_audit=256, seed=0, dims
         t_refine += time.perf_counter() - t0
         if new:
             new = np.array(new)
-            y_new, t_new = simulate(q1[new], q2[new], dT[new], da[new], dims, steps, device=device)
+            y_new, t_new = sim(new)
             t_refine += t_new
             for i, v in zip(new.tolist(), bounded(y_new)[:, objective].tolist()):
                 known[i] = v
@@ -152,7 +173,7 @@ def screen(n_candidates=65536, n_train=512, top_k=256, n_audit=256, seed=0, dims
     screened = t_train + t_fit + t_pred + t_chk + t_refine
     report["gpu_seconds"]["screened_total"] = screened
     if exhaustive:
-        y_all, t_all = simulate(q1, q2, dT, da, dims, steps, device=device)
+        y_all, t_all = sim(np.arange(n_candidates))
         y_all = bounded(y_all)
         truth = y_all[:, objective]
         fin = np.isfinite(truth)
