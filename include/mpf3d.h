@@ -375,7 +375,9 @@ int mpf3d_batched_ray_radii(const uint32_t *head, const uint16_t *idx, const flo
  * B(k,n) = B[k*sbk + n*sbn]; act 0 = none, 1 = SiLU.  Z (nullable) receives
  * the FP32 pre-activation, Y the result (BF16 if y_bf16, else FP32, added to
  * Y when beta = 1), both with row stride ldy.  K-major operands that fit
- * mpf3d_gemm_bf16_tc5 run there, the rest on mpf3d_gemm_bf16_mma.  err
+ * mpf3d_gemm_bf16_tc5 run there, other layouts on
+ * mpf3d_gemm_bf16_tc5_strided, shapes neither covers on
+ * mpf3d_gemm_bf16_mma.  err
  * (nullable device word) receives MPF3D_DEV_GEMM_ABORT from the tcgen05
  * kernel. */
 int mpf3d_gemm_bf16(int M, int N, int K, const uint16_t *A, int64_t sam, int64_t sak, const uint16_t *B,
@@ -395,6 +397,17 @@ int mpf3d_gemm_bf16(int M, int N, int K, const uint16_t *A, int64_t sam, int64_t
 int mpf3d_gemm_bf16_tc5(int M, int N, int K, const uint16_t *A, int64_t lda, const uint16_t *B, int64_t ldb,
                         const float *bias, int act, float *Z, void *Y, int ldy, int y_bf16, int beta, int32_t *err,
                         void *stream);
+
+/* The tcgen05 kernel for operands in any layout -- A(m,k) = A[m*sam + k*sak],
+ * B(k,n) = B[k*sbk + n*sbn] as in mpf3d_gemm_bf16 -- which gathers them into
+ * the K-major shared-memory layout (the gradients dZ W and dZ^T X of the
+ * surrogate read transposed operands).  N <= 256, any K: the reduction is
+ * staged in blocks of up to 256 (zero-padded to a multiple of 16), and a
+ * reduction deeper than 256 is accumulated block by block into an FP32 Y
+ * (then act must be 0, Z null and y_bf16 0). */
+int mpf3d_gemm_bf16_tc5_strided(int M, int N, int K, const uint16_t *A, int64_t sam, int64_t sak, const uint16_t *B,
+                                int64_t sbk, int64_t sbn, const float *bias, int act, float *Z, void *Y, int ldy,
+                                int y_bf16, int beta, int32_t *err, void *stream);
 
 /* The pipelined tcgen05 kernel of mpf3d_gemm_bf16_tc5 (K a multiple of 64)
  * with its TMA producer held back, so that no copy and no MMA is ever issued

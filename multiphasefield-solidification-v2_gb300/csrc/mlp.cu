@@ -289,14 +289,21 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
     asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
 }
 
-__device__ __forceinline__ void stage(uint8_t *dst, const uint16_t *__restrict__ src, int64_t ld, int rows_valid,
-                                      int rows, int K) {
+// Stages rows x K of an operand into the K-major core-matrix layout:
+// element (r, k) is src[r * s_row + k * s_k]; rows at or past rows_valid
+// and columns at or past K_valid are zero.  With s_k == 1 (K contiguous in
+// global memory) the chunks of 8 columns are 16-byte loads; otherwise (a
+// transposed operand: the gradients' dZ^T, X^T and W^T) they are gathered
+// element by element, consecutive threads on consecutive rows.
+__device__ __forceinline__ void stage(uint8_t *dst, const uint16_t *__restrict__ src, int64_t s_row, int64_t s_k,
+                                      int rows_valid, int rows, int K, int K_valid) {
     // chunk e is row (e % 8) of core (e / 8): 8 consecutive threads fill one
     // 128-byte core matrix; 8 chunks per thread are loaded before any is
     // stored, so the loads overlap
     const int kc = K / 8;
     const uint32_t sbo = (uint32_t)kc * 128u;
     const int total = rows * kc;
+    const bool vec = s_k == 1 && K_valid == K && (s_row % 8) == 0 && (((uintptr_t)src & 15u) == 0);
     constexpr int U = 8;
     for (int e0 = threadIdx.x; e0 < total; e0 += U * blockDim.x) {
         uint4 v[U];
@@ -308,7 +315,22 @@ __device__ __forceinline__ void stage(uint8_t *dst, const uint16_t *__restrict__
                 const int core = e >> 3, r8 = e & 7;
                 const int rb = core / kc, c = core - rb * kc;
                 const int r = rb * 8 + r8;
-                if (r < rows_valid) v[u] = __ldg(reinterpret_cast<const uint4 *>(src + (int64_t)r * ld + c * 8));
+                if (r < rows_valid) {
+                    if (vec) {
+                        v[u] = __ldg(reinterpret_cast<const uint4 *>(src + (int64_t)r * s_row + c * 8));
+                    } else {
+                        uint32_t w[4];
+#pragma unroll
+                        for (int j = 0; j < 4; ++j) {
+                            const int k0 = c * 8 + 2 * j;
+                            const uint32_t lo = k0 < K_valid ? __ldg(src + (int64_t)r * s_row + (int64_t)k0 * s_k) : 0u;
+                            const uint32_t hi =
+                                k0 + 1 < K_valid ? __ldg(src + (int64_t)r * s_row + (int64_t)(k0 + 1) * s_k) : 0u;
+                            w[j] = lo | (hi << 16);
+                        }
+                        v[u] = make_uint4(w[0], w[1], w[2], w[3]);
+                    }
+                }
             }
         }
 #pragma unroll
@@ -324,11 +346,13 @@ __device__ __forceinline__ void stage(uint8_t *dst, const uint16_t *__restrict__
 }
 
 // Persistent CTAs: each stages B once, then loops over 128-row tiles of A.
-__global__ void __launch_bounds__(128) gemm_kernel(int M, int N, int K, const uint16_t *__restrict__ A, int64_t lda,
-                                                   const uint16_t *__restrict__ B, int64_t ldb,
-                                                   const float *__restrict__ bias, int act, float *__restrict__ Z,
-                                                   void *__restrict__ Y, int ldy, int y_bf16, int beta,
-                                                   int32_t *__restrict__ err) {
+// A(m, k) = A[m * sam + k * sak] and B(n, k) = B[n * sbn + k * sbk] for
+// k < K_valid; K (a multiple of 16) >= K_valid is the staged depth.
+__global__ void __launch_bounds__(128) gemm_kernel(int M, int N, int K, int K_valid, const uint16_t *__restrict__ A,
+                                                   int64_t sam, int64_t sak, const uint16_t *__restrict__ B,
+                                                   int64_t sbn, int64_t sbk, const float *__restrict__ bias, int act,
+                                                   float *__restrict__ Z, void *__restrict__ Y, int ldy, int y_bf16,
+                                                   int beta, int32_t *__restrict__ err) {
     extern __shared__ __align__(1024) uint8_t smem[];
     const int n_mma = (N + 15) & ~15;
     uint8_t *sA = smem;
@@ -349,7 +373,7 @@ __global__ void __launch_bounds__(128) gemm_kernel(int M, int N, int K, const ui
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
     }
-    stage(sB, B, ldb, N, n_mma, K);
+    stage(sB, B, sbn, sbk, N, n_mma, K, K_valid);
     const uint32_t bar_a = smem_addr(bar);
     const uint32_t idesc = instr_desc(TM, n_mma);
     const uint32_t a0 = smem_addr(sA), b0 = smem_addr(sB), sbo = (uint32_t)(K / 8) * 128u;
@@ -359,7 +383,7 @@ __global__ void __launch_bounds__(128) gemm_kernel(int M, int N, int K, const ui
     int it = 0;
     for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x, ++it) {
         const int m0 = tile * TM;
-        stage(sA, A + (int64_t)m0 * lda, lda, min(TM, M - m0), TM, K);
+        stage(sA, A + (int64_t)m0 * sam, sam, sak, min(TM, M - m0), TM, K, K_valid);
         // the tensor core reads shared memory through the async proxy; the
         // previous tile's accumulator reads are complete (barrier below)
         asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
@@ -844,9 +868,38 @@ extern "C" int mpf3d_gemm_bf16_tc5(int M, int N, int K, const uint16_t *A, int64
     const int tiles = (M + tc5::TM - 1) / tc5::TM;
     const int per_sm = bytes > 114 * 1024 ? 1 : 2;
     const int grid = tiles < sms_of_device() * per_sm ? tiles : sms_of_device() * per_sm;
-    tc5::gemm_kernel<<<grid, 128, bytes, (cudaStream_t)stream>>>(M, N, K, A, lda, B, ldb, bias, act, Z, Y, ldy,
-                                                                 y_bf16, beta, err);
+    tc5::gemm_kernel<<<grid, 128, bytes, (cudaStream_t)stream>>>(M, N, K, K, A, lda, 1, B, ldb, 1, bias, act, Z, Y,
+                                                                 ldy, y_bf16, beta, err);
     return cudaGetLastError() == cudaSuccess ? MPF3D_OK : MPF3D_ERR_CUDA;
+}
+
+extern "C" int mpf3d_gemm_bf16_tc5_strided(int M, int N, int K, const uint16_t *A, int64_t sam, int64_t sak,
+                                           const uint16_t *B, int64_t sbk, int64_t sbn, const float *bias, int act,
+                                           float *Z, void *Y, int ldy, int y_bf16, int beta, int32_t *err,
+                                           void *stream) {
+    using namespace mpf3d::mlp;
+    if (M <= 0 || N <= 0 || N > tc5::MAX_N || K <= 0 || !A || !B || !Y || ldy < N || (act != 0 && act != 1))
+        return MPF3D_ERR_ARG;
+    const int chunks = (K + tc5::MAX_K - 1) / tc5::MAX_K;
+    // a reduction deeper than one staged block is accumulated chunk by chunk
+    // into an FP32 result: no activation, no pre-activation output
+    if (chunks > 1 && (act != 0 || Z || y_bf16)) return MPF3D_ERR_ARG;
+    const size_t bytes = tc5::smem_bytes(N, K < tc5::MAX_K ? ((K + 15) & ~15) : tc5::MAX_K);
+    if (cudaFuncSetAttribute(tc5::gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) !=
+        cudaSuccess)
+        return MPF3D_ERR_CUDA;
+    const int tiles = (M + tc5::TM - 1) / tc5::TM;
+    const int per_sm = bytes > 114 * 1024 ? 1 : 2;
+    const int grid = tiles < sms_of_device() * per_sm ? tiles : sms_of_device() * per_sm;
+    for (int c = 0; c < chunks; ++c) {
+        const int k0 = c * tc5::MAX_K;
+        const int kv = K - k0 < tc5::MAX_K ? K - k0 : tc5::MAX_K;
+        tc5::gemm_kernel<<<grid, 128, bytes, (cudaStream_t)stream>>>(
+            M, N, (kv + 15) & ~15, kv, A + (int64_t)k0 * sak, sam, sak, B + (int64_t)k0 * sbk, sbn, sbk,
+            c == 0 ? bias : nullptr, act, Z, Y, ldy, y_bf16, c == 0 ? beta : 1, err);
+        if (cudaGetLastError() != cudaSuccess) return MPF3D_ERR_CUDA;
+    }
+    return MPF3D_OK;
 }
 
 extern "C" int mpf3d_gemm_bf16_tc5_held(int M, int N, int K, const uint16_t *A, int64_t lda, const uint16_t *B,
@@ -874,10 +927,15 @@ extern "C" int mpf3d_gemm_bf16_mma(int M, int N, int K, const uint16_t *A, int64
 extern "C" int mpf3d_gemm_bf16(int M, int N, int K, const uint16_t *A, int64_t sam, int64_t sak, const uint16_t *B,
                                int64_t sbk, int64_t sbn, const float *bias, int act, float *Z, void *Y, int ldy,
                                int y_bf16, int beta, int32_t *err, void *stream) {
-    // K-major operands (the forward pass X W^T) go to the tcgen05 kernel;
-    // transposed ones (the gradients) to the mma.sync kernel
+    // K-major operands (the forward pass X W^T) go to the pipelined tcgen05
+    // kernel; transposed ones (the gradients dZ W and dZ^T X) to the tcgen05
+    // kernel that gathers them into the K-major layout; shapes neither covers
+    // to the mma.sync kernel
     if (sak == 1 && sbk == 1 && tc5_shape_ok(M, N, K, A, sam, B, sbn))
         return mpf3d_gemm_bf16_tc5(M, N, K, A, sam, B, sbn, bias, act, Z, Y, ldy, y_bf16, beta, err, stream);
+    if (N <= mpf3d::mlp::tc5::MAX_N && (K <= mpf3d::mlp::tc5::MAX_K || (act == 0 && !Z && !y_bf16)))
+        return mpf3d_gemm_bf16_tc5_strided(M, N, K, A, sam, sak, B, sbk, sbn, bias, act, Z, Y, ldy, y_bf16, beta, err,
+                                           stream);
     return mpf3d_gemm_bf16_mma(M, N, K, A, sam, sak, B, sbk, sbn, bias, act, Z, Y, ldy, y_bf16, beta, stream);
 }
 

@@ -93,6 +93,8 @@ _SIGS = {
                                _I32, _I32, _VP]),
     "mpf3d_gemm_bf16_tc5": (_I32, [_I32, _I32, _I32, _VP, _I64, _VP, _I64, _VP, _I32, _VP, _VP, _I32, _I32, _I32,
                                    _VP, _VP]),
+    "mpf3d_gemm_bf16_tc5_strided": (_I32, [_I32, _I32, _I32, _VP, _I64, _I64, _VP, _I64, _I64, _VP, _I32, _VP, _VP,
+                                           _I32, _I32, _I32, _VP, _VP]),
     "mpf3d_gemm_bf16_tc5_held": (_I32, [_I32, _I32, _I32, _VP, _I64, _VP, _I64, _VP, _I32, _VP, ctypes.c_uint64,
                                         _VP]),
     "mpf3d_act_backward": (_I32, [_VP, _VP, _I32, _I64, _VP, _VP, _VP]),

@@ -5,9 +5,11 @@ velocity ratio and the grain-boundary inclination.
 
 Weights are stored in FP32 (Adam master copy) and BF16 (the copy the
 tensor-core GEMMs read); every matrix product runs in libmpf3d's
-`mpf3d_gemm_bf16` (mma.sync m16n8k16, FP32 accumulate), the activation
-derivative, loss and Adam in its elementwise kernels.  Torch provides device
-memory only.
+`mpf3d_gemm_bf16` on the fifth-generation tensor cores (tcgen05, FP32
+accumulate in tensor memory): the forward products X W^T on the TMA-fed
+pipelined kernel, the gradients dZ W and dZ^T X on the kernel that gathers
+transposed operands into shared memory.  The activation derivative, loss and
+Adam run in its elementwise kernels.  Torch provides device memory only.
 
 No reference counterpart: the reference has no learned component; it scans
 orientations one simulation at a time (run_orientation_scan_3d.py:686-841).

@@ -1,7 +1,8 @@
-"""Surrogate network kernels on the GPU: the BF16 tensor-core GEMM against a
+"""Surrogate network kernels on the GPU: the BF16 tensor-core GEMMs against a
 float64 product of the same BF16 operands (all operand layouts the network
-uses), the full backward pass against a CPU float64 restatement with the same
-BF16 rounding points, and training on a smooth target."""
+uses, forward and gradients on tcgen05), the full backward pass against a
+CPU float64 restatement with the same BF16 rounding points, and training on
+a smooth target."""
 import numpy as np
 import pytest
 
@@ -95,6 +96,39 @@ def test_tcgen05_gemm_matches_float64(M, N, K, act, y_bf16):
         assert np.abs(Y.cpu().numpy() - Y2.cpu().numpy()).max() <= 1e-4 * scale * np.sqrt(K)
 
 
+@pytest.mark.parametrize("M,N,K,transA,transB,beta", [(256, 256, 600, True, False, 0), (2, 256, 512, True, False, 1),
+                                                      (512, 256, 2, False, True, 0), (300, 16, 256, True, False, 0),
+                                                      (512, 256, 256, False, True, 1), (77, 200, 40, True, True, 0)])
+def test_tcgen05_gradient_gemm_matches_float64(M, N, K, transA, transB, beta):
+    """The tcgen05 kernel for transposed operands (the surrogate's gradients:
+    dW = dZ^T X with the batch as reduction, dH = dZ W with W read across its
+    rows), against a float64 product of the same BF16 operands: reductions
+    deeper than one 256-deep block (accumulated block by block), reductions
+    padded to a multiple of 16, and accumulation into the output (beta)."""
+    from mpf3d import _lib
+    rng = np.random.default_rng(M * 3 + N + K)
+    A = rng.standard_normal((M, K)).astype(np.float32)
+    B = rng.standard_normal((K, N)).astype(np.float32)
+    A_store = A.T.copy() if transA else A
+    B_store = B.T.copy() if transB else B
+    sam, sak = (1, M) if transA else (K, 1)
+    sbk, sbn = (1, K) if transB else (N, 1)
+    dev = torch.device("cuda:0")
+    tA = torch.from_numpy(to_bf16_bits(A_store)).to(dev)
+    tB = torch.from_numpy(to_bf16_bits(B_store)).to(dev)
+    Y0 = rng.standard_normal((M, N)).astype(np.float32)
+    Y = torch.from_numpy(Y0.copy()).to(dev)
+    err = torch.zeros(1, dtype=torch.int32, device=dev)
+    rc = _lib.lib().mpf3d_gemm_bf16_tc5_strided(M, N, K, tA.data_ptr(), sam, sak, tB.data_ptr(), sbk, sbn, None, 0,
+                                                None, Y.data_ptr(), N, 0, beta, err.data_ptr(), None)
+    assert rc == 0
+    torch.cuda.synchronize()
+    assert int(err.item()) == 0
+    ref = bf16_round(A) @ bf16_round(B) + (Y0 if beta else 0.0)
+    scale = np.abs(bf16_round(A) @ bf16_round(B)).max()
+    assert np.abs(Y.cpu().numpy() - ref).max() <= 1e-5 * scale * np.sqrt(K)
+
+
 def test_tcgen05_rejects_shapes_it_does_not_cover():
     from mpf3d import _lib
     L = _lib.lib()
@@ -102,6 +136,11 @@ def test_tcgen05_rejects_shapes_it_does_not_cover():
     assert L.mpf3d_gemm_bf16_tc5(64, 300, 64, p, 64, p, 64, None, 0, None, p, 300, 0, 0, None, None) == -1  # N > 256
     assert L.mpf3d_gemm_bf16_tc5(64, 64, 24, p, 24, p, 24, None, 0, None, p, 64, 0, 0, None, None) == -1    # K % 16
     assert L.mpf3d_gemm_bf16_tc5(64, 64, 512, p, 512, p, 512, None, 0, None, p, 64, 0, 0, None, None) == -1  # K > 256
+    # a reduction deeper than 256 accumulates into FP32: no activation, no Z, no BF16 output
+    assert L.mpf3d_gemm_bf16_tc5_strided(64, 64, 512, p, 1, 64, p, 1, 512, None, 1, None, p, 64, 0, 0, None,
+                                         None) == -1
+    assert L.mpf3d_gemm_bf16_tc5_strided(64, 64, 512, p, 1, 64, p, 1, 512, None, 0, None, p, 64, 1, 0, None,
+                                         None) == -1
 
 
 def test_tcgen05_abort_path_reports_and_frees():
