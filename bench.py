@@ -334,9 +334,9 @@ def run_ours(args, rank, world):
     solver.step(args.warmup)
     tuned = solver.autotune(steps=8) if not args.no_autotune else None
     torch.cuda.synchronize(dev)
-    tuning = solver.tuning
+    tuning, sweep_tma = solver.tuning, solver.sweep_tma
     solver = CompactSolver(phi0, temp, n111, wij, aij, mij, phys, slots=args.slots)
-    solver.tuning = tuning
+    solver.tuning, solver.sweep_tma = tuning, sweep_tma
     torch.cuda.synchronize(dev)
 
     e0 = torch.cuda.Event(enable_timing=True)
@@ -359,7 +359,7 @@ def run_ours(args, rank, world):
     # the new one; cells of tiles skipped as quiet move nothing), the quiet
     # share and the stored-phase occupancy
     acc = CompactSolver(phi0, temp, n111, wij, aij, mij, phys, slots=args.slots)
-    acc.tuning = tuning
+    acc.tuning, acc.sweep_tma = tuning, sweep_tma
     occ = [int(acc.stored_counts().sum(dtype=torch.int64).item())]
     rec_all = 0
     bytes_total = 0
@@ -391,10 +391,10 @@ def run_ours(args, rank, world):
 
     # end to end through the public API: pinned dense phi in, dense phi out
     if args.no_e2e:
-        t_e2e, in_bytes, out_bytes = float("nan"), 0, 0
+        t_e2e, in_bytes, out_bytes, t_staged = float("nan"), 0, 0, float("nan")
     else:
-        t_e2e, in_bytes, out_bytes = e2e_run(args, phi0, temp, n111, wij, aij, mij, phys, dev, barrier, world,
-                                             tuning)
+        t_e2e, in_bytes, out_bytes, t_staged = e2e_run(args, phi0, temp, n111, wij, aij, mij, phys, dev, barrier,
+                                                       world, tuning, sweep_tma)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -402,7 +402,11 @@ def run_ours(args, rank, world):
         cpu = {"value": v, "unit": UNIT, "cores": th, "kind": "port",
                "sample": f"64x64x256 crop of the workload (N=65), {st} oracle steps (reference "
                          f"float32 typing), OpenMP"}
-    extra = {"launch_shape": {"config": list(tuned["config"]), "ms_per_step_tuned": tuned["ms_per_step"],
+    extra = {"e2e_staged_copies": {"value": cells * args.steps * world / t_staged, "unit": UNIT,
+                                   "note": "the same job with dense phi copied to device memory and back "
+                                           "(cudaMemcpy of pinned buffers) instead of converted in place"},
+             "launch_shape": {"config": list(tuned["config"]), "sweep_tma": bool(sweep_tma),
+                              "ms_per_step_tuned": tuned["ms_per_step"],
                               "ms_per_step_default": tuned["default_ms_per_step"]} if tuned else None}
     if rank == 0 and not args.no_accuracy and args.accuracy_steps > 0:
         del solver
@@ -423,36 +427,47 @@ def run_ours(args, rank, world):
                                                                          full_state_bytes / cells))
 
 
-def e2e_run(args, phi0, temp, n111, wij, aij, mij, phys, dev, barrier, world, tuning=None):
+def e2e_run(args, phi0, temp, n111, wij, aij, mij, phys, dev, barrier, world, tuning=None, sweep_tma=False):
     import torch
     from mpf3d.solver import CompactSolver
     phi_host = phi0.cpu().pin_memory()
     out_host = torch.empty_like(phi_host).pin_memory()
 
-    def job(steps):
-        dphi = phi_host.to(dev, non_blocking=True)
-        s2 = CompactSolver(dphi, temp, n111, wij, aij, mij, phys, slots=args.slots)
-        s2.tuning = tuning
+    def job(steps, staged=False):
+        if staged:
+            # staging copies: dense phi copied to device memory and back
+            dphi = phi_host.to(dev, non_blocking=True)
+            s2 = CompactSolver(dphi, temp, n111, wij, aij, mij, phys, slots=args.slots)
+        else:
+            # the converters read and write the pinned host buffers in place
+            s2 = CompactSolver(phi_host, temp, n111, wij, aij, mij, phys, slots=args.slots)
+        s2.tuning, s2.sweep_tma = tuning, sweep_tma
         s2.step(steps, check=False)
-        out_host.copy_(s2.to_dense(host=False), non_blocking=True)
+        if staged:
+            out_host.copy_(s2.to_dense(host=False), non_blocking=True)
+        else:
+            s2.to_dense(out=out_host)
         return s2
 
-    # untimed warm-up pass of the same sequence: the first 4.4 GB device
-    # allocations of a process cost a box-dependent 20-70 ms that a user
-    # submitting jobs pays once; the timed pass keeps every copy
-    job(args.warmup).check()
-    torch.cuda.synchronize(dev)
-    barrier()
-    t0 = time.perf_counter()
-    s2 = job(args.steps)
-    torch.cuda.synchronize(dev)
-    t_e2e = time.perf_counter() - t0
-    s2.check()
-    barrier()
-    t_e2e = max_over_ranks(t_e2e, world)
+    times = {}
+    for staged in (False, True):
+        # untimed warm-up pass of the same sequence: the first 4.4 GB device
+        # allocations of a process cost a box-dependent 20-70 ms that a user
+        # submitting jobs pays once; the timed pass keeps every copy
+        job(args.warmup, staged).check()
+        torch.cuda.synchronize(dev)
+        barrier()
+        t0 = time.perf_counter()
+        s2 = job(args.steps, staged)
+        torch.cuda.synchronize(dev)
+        times[staged] = time.perf_counter() - t0
+        s2.check()
+        del s2
+        barrier()
+    t_e2e = max_over_ranks(times[False], world)
     in_bytes = phi_host.numel() * 4 + temp.nbytes + n111.nbytes + 3 * wij.nbytes
     out_bytes = out_host.numel() * 4
-    return t_e2e, in_bytes, out_bytes
+    return t_e2e, in_bytes, out_bytes, max_over_ranks(times[True], world)
 
 
 def dense_reference_rate(phi0, temp, n111, wij, aij, mij, phys, dev, steps=20):
@@ -649,7 +664,9 @@ def divergence_study(phi0, temp, n111, wij, aij, mij, phys, dev, steps, slots=16
     def noise_1ulp(p):
         r = torch.rand(p.shape, generator=gen, device=dev, dtype=torch.float32)
         inner = (p > 0) & (p < 1)
-        p.copy_(torch.where(inner, p * torch.where(r < 0.5, 1.0 - 2.0 ** -52, 1.0 + 2.0 ** -52).double(), p))
+        # the factor 1 +- 2^-52 formed in float64 (a float32 scalar would round it to 1)
+        factor = 1.0 + torch.where(r < 0.5, -1.0, 1.0).double() * 2.0 ** -52
+        p.copy_(torch.where(inner, p * factor, p))
 
     ref = Dense(torch.float64, False)
     runs = {"f32_reference_numerics": Dense(torch.float32, True), "fp64_fp32_storage": Dense(torch.float64, False),
@@ -873,8 +890,9 @@ def run_c3(args):
 
 
 def run_accuracy_study(args):
-    """The FP32-vs-FP64 error trajectory of the 256^3 workload over --steps
-    steps (default bench runs only the first 100)."""
+    """The FP32-vs-FP64 divergence study of the bench workload (or of the
+    grid, grains and slab given) over --steps steps (the default bench line
+    runs only the first 100)."""
     import torch
     from mpf3d import inputs
     dev = torch.device("cuda:0")
@@ -920,15 +938,20 @@ def main():
     ap.add_argument("--c5-config", action="store_true",
                     help="c5: instances of {64,96,128}^2 x {64,96} cells stepped 3000 steps (the stated "
                          "configuration) instead of 32x32x64 for 300 steps")
+    ap.add_argument("--slab", type=int, default=None,
+                    help="height of the solid Voronoi slab and of the initial front (default 32; the "
+                         "1024x1024x256 workload uses 24)")
     ap.add_argument("--grains", type=int, default=None,
                     help="grains of the Voronoi slab (default 64; a crop of the 256^3 workload keeps the grain "
                          "density with 64 * nx * ny / 256^2)")
     args = ap.parse_args()
-    global GRID, N_GRAINS
+    global GRID, N_GRAINS, SLAB
     if args.grid:
         GRID = tuple(args.grid)
     if args.grains:
         N_GRAINS = int(args.grains)
+    if args.slab:
+        SLAB = int(args.slab)
     if args.warmup < 3:
         args.warmup = 3
     world = int(os.environ.get("WORLD_SIZE", "1"))

@@ -42,6 +42,8 @@ extern "C" {
 #define MPF3D_DEV_SLOT_OVERFLOW 8 /* compact stepper: more phases than slots */
 #define MPF3D_DEV_BAD_INPUT 16    /* compact conversion met a negative/NaN phi */
 #define MPF3D_DEV_GEMM_ABORT 32   /* tcgen05 GEMM: a bounded wait ran out; the CTA's outputs are NaN */
+#define MPF3D_DEV_STAGING_TIMEOUT 64 /* compact step: a TMA staging copy did not land in time (the block's
+                                      * cells were not processed) */
 
 /* compile-time bound on active phases per cell (reference KMAX) */
 #define MPF3D_KMAX 50
@@ -122,6 +124,14 @@ int mpf2d_dense_temp(void *temp, int temp_dtype, double cooling_rate, int rate_i
  * cell set MPF3D_DEV_SLOT_OVERFLOW. */
 int mpf3d_compact_from_dense(const void *phi, int phi_dtype, int N, int nx, int ny, int nz, int slots,
                              uint32_t *head, uint16_t *idx, float *val, int32_t *err, void *stream);
+
+/* Device address of page-locked (pinned) host memory, for the converters
+ * below: with it mpf3d_compact_from_dense reads dense phi straight from
+ * host memory and mpf3d_compact_to_dense writes it straight back, over the
+ * CPU-GPU link, with no staging copy in device memory.  MPF3D_ERR_ARG when
+ * `host` is not page-locked.  No reference counterpart (the reference copies
+ * whole device arrays with cuda.to_device / copy_to_host). */
+int mpf3d_host_device_pointer(const void *host, void **device);
 
 /* compact state -> dense phi (every phase written, zeros included). */
 int mpf3d_compact_to_dense(const uint32_t *head, const uint16_t *idx, const float *val, int slots, int N,
@@ -207,8 +217,8 @@ typedef struct mpf3d_tuning {
  * the output buffer already holds its cells.  The result is identical to
  * tile_flags = NULL.  Zero the whole array whenever the state buffers are
  * written other than by this function (initialisation, restore, rollback)
- * or sweep_zb changes; steps must alternate parity.  options: 0 or
- * MPF3D_STEP_MULTI_LIST. */
+ * or sweep_zb changes; steps must alternate parity.  options: an OR of
+ * MPF3D_STEP_MULTI_LIST and MPF3D_STEP_SWEEP_TMA. */
 int mpf3d_compact_step_tuned(const uint32_t *head, const uint16_t *idx, const float *val, uint32_t *head_out,
                              uint16_t *idx_out, float *val_out, int slots, int amax, const double *T0z,
                              double Tm_plus_cool, const float *wij, const float *a2ij, const float *mij,
@@ -222,6 +232,11 @@ int mpf3d_compact_step_tuned(const uint32_t *head, const uint16_t *idx, const fl
                                  * from the heads) get a work list of their own at
                                  * work_items[cells .. 2*cells): work_items must then hold 2*cells
                                  * entries and work_count 6.  Same results, fewer idle lanes. */
+
+#define MPF3D_STEP_SWEEP_TMA 2 /* the sweep stages each block's heads plus a one-cell halo in shared memory
+                                * with one TMA copy (cp.async.bulk.tensor.3d) and classifies from there;
+                                * needs nx a multiple of 4 (otherwise the plain sweep runs).  Same
+                                * results. */
 
 /* Bytes of tile_flags for an nx x ny x nz domain (any sweep_zb). */
 int64_t mpf3d_compact_tile_flags_len(int nx, int ny, int nz);

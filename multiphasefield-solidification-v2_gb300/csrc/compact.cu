@@ -23,6 +23,8 @@
 // Temperature is T0[z] - (accumulated cooling) with the accumulator in
 // float64 on the host; the per-cell sum-to-one uses a compensated float
 // pair (TwoSum), which keeps GB300's slow float64 pipe out of the loop.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdint.h>
@@ -232,10 +234,24 @@ __device__ __forceinline__ uint32_t cidx(const Params &P, int l, int m, int k) {
     return P.base + ((uint32_t)k * (uint32_t)P.ny + (uint32_t)m) * (uint32_t)P.nx + (uint32_t)l;
 }
 
+// liquid fraction of cell q; the head and the first value are loaded
+// together (the value is ignored where the head says it is not needed), so
+// the liquid stencil costs one round of loads rather than two
 __device__ __forceinline__ float liquid32(const In &in, uint32_t q) {
     const uint32_t h = __ldg(in.head + q);
+    const float v = __ldg(in.val + q);
     if (hcount(h) == 0 || hid0(h) != LIQ) return 0.0f;
-    return value0(in, h, q);
+    return (hcount(h) >= 2 || hexplicit(h)) ? v : 1.0f;
+}
+
+// 7-point Laplacian of one phase, rounded operation by operation
+__device__ __forceinline__ float lap7(const Params &P, const float (&v)[7]) {
+    float s = __fadd_rn(v[1], v[2]);
+    s = __fadd_rn(s, v[3]);
+    s = __fadd_rn(s, v[4]);
+    s = __fadd_rn(s, v[5]);
+    s = __fadd_rn(s, v[6]);
+    return __fmul_rn(__fsub_rn(s, __fmul_rn(6.0f, v[0])), P.inv_dx2);
 }
 
 // Active list of one cell: the ascending union of the stored lists of the
@@ -294,7 +310,7 @@ __device__ __forceinline__ void gather(const In &in, const Params &P, const uint
         }
         A.ids[A.n] = id;
         A.vc[A.n] = v[0];
-        A.lap[A.n] = (v[1] + v[2] + v[3] + v[4] + v[5] + v[6] - 6.0f * v[0]) * P.inv_dx2;
+        A.lap[A.n] = lap7(P, v);
         if (id == LIQ) {
 #pragma unroll
             for (int p = 0; p < 7; ++p) A.vL[p] = v[p];
@@ -411,8 +427,190 @@ __device__ __forceinline__ void interface_terms(const Params &P, const float3 (&
     b_sl = calc_b(P, G[0], F[0]);
 }
 
-// Update of one cell whose neighbourhood is not uniform.  HEAVY enables the
-// anisotropic solid-liquid terms (cells with liquid and a solid active).
+// Everything of the update of one cell after its active list is known:
+// ids (ascending), values vc and Laplacians lap of the n active phases, the
+// liquid at the 7 points, and the dominant solid ts (index, -1 if none) with
+// its gradient gs.  HEAVY enables the anisotropic solid-liquid terms (cells
+// with liquid and a solid active).  The per-phase loops are kept rolled:
+// unrolled copies of this body made the kernels wait on instruction fetch.
+template <int S, int NA, bool HEAVY>
+__device__ __forceinline__ void update_cell(const In &in, const Out &out, const Mats &M, const Params &P, int l,
+                                            int m, int k, uint32_t c, int n, const int (&ids)[NA],
+                                            const float (&vc)[NA], const float (&lap)[NA], const float (&vL)[7],
+                                            int ts, float3 gs, int32_t *__restrict__ err) {
+    const uint32_t cells = P.cells32;
+    const int nn = n;
+    const bool has_liq = n > 0 && ids[0] == LIQ;
+    const bool has_solid = n > (has_liq ? 1 : 0);
+    float lap_sl[NA], b_sl[NA];
+    float w_sl = P.w0;
+    lap_sl[0] = 0.0f;
+    b_sl[0] = 1.0f;
+    if (has_liq && has_solid) {
+        if (HEAVY && P.use_aniso) {
+            const int lp = wrap_p(l, P.nx), lm = wrap_m(l, P.nx), mp = wrap_p(m, P.ny), mm = wrap_m(m, P.ny);
+            const int kp = clamp_p(k, P.nz), km = clamp_m(k, P.nz);
+            // liquid on the 25-point stencil (offsets with |dx|+|dy|+|dz| <= 2)
+            const int lpp = wrap_p(lp, P.nx), lmm = wrap_m(lm, P.nx);
+            const int mpp = wrap_p(mp, P.ny), mmm = wrap_m(mm, P.ny);
+            const int kpp = clamp_p(kp, P.nz), kmm = clamp_m(km, P.nz);
+            const float Lxpyp = liquid32(in, cidx(P, lp, mp, k)), Lxpym = liquid32(in, cidx(P, lp, mm, k));
+            const float Lxmyp = liquid32(in, cidx(P, lm, mp, k)), Lxmym = liquid32(in, cidx(P, lm, mm, k));
+            const float Lxpzp = liquid32(in, cidx(P, lp, m, kp)), Lxpzm = liquid32(in, cidx(P, lp, m, km));
+            const float Lxmzp = liquid32(in, cidx(P, lm, m, kp)), Lxmzm = liquid32(in, cidx(P, lm, m, km));
+            const float Lypzp = liquid32(in, cidx(P, l, mp, kp)), Lypzm = liquid32(in, cidx(P, l, mp, km));
+            const float Lymzp = liquid32(in, cidx(P, l, mm, kp)), Lymzm = liquid32(in, cidx(P, l, mm, km));
+            const float Lx2p = liquid32(in, cidx(P, lpp, m, k)), Lx2m = liquid32(in, cidx(P, lmm, m, k));
+            const float Ly2p = liquid32(in, cidx(P, l, mpp, k)), Ly2m = liquid32(in, cidx(P, l, mmm, k));
+            const float Lz2p = liquid32(in, cidx(P, l, m, kpp)), Lz2m = liquid32(in, cidx(P, l, m, kmm));
+            const float g2 = P.inv_2dx;
+            float3 G[7];
+            G[0] = make_float3((vL[1] - vL[2]) * g2, (vL[3] - vL[4]) * g2, (vL[5] - vL[6]) * g2);
+            G[1] = make_float3((Lx2p - vL[0]) * g2, (Lxpyp - Lxpym) * g2, (Lxpzp - Lxpzm) * g2);
+            G[2] = make_float3((vL[0] - Lx2m) * g2, (Lxmyp - Lxmym) * g2, (Lxmzp - Lxmzm) * g2);
+            G[3] = make_float3((Lxpyp - Lxmyp) * g2, (Ly2p - vL[0]) * g2, (Lypzp - Lypzm) * g2);
+            G[4] = make_float3((Lxpym - Lxmym) * g2, (vL[0] - Ly2m) * g2, (Lymzp - Lymzm) * g2);
+            // z neighbours sit on the clamped rows: at the top/bottom row the
+            // neighbour is the cell itself
+            G[5] = (kp == k) ? G[0] : make_float3((Lxpzp - Lxmzp) * g2, (Lypzp - Lymzp) * g2, (Lz2p - vL[0]) * g2);
+            G[6] = (km == k) ? G[0] : make_float3((Lxpzm - Lxmzm) * g2, (Lypzm - Lymzm) * g2, (vL[0] - Lz2m) * g2);
+            if (kp == k) G[5].z = (vL[5] - vL[6]) * g2;
+            if (km == k) G[6].z = (vL[5] - vL[6]) * g2;
+            float h2[6];
+            const float qq = 0.25f * P.inv_dx2;
+            h2[0] = (vL[1] - 2.0f * vL[0] + vL[2]) * P.inv_dx2;
+            h2[1] = (vL[3] - 2.0f * vL[0] + vL[4]) * P.inv_dx2;
+            h2[2] = (vL[5] - 2.0f * vL[0] + vL[6]) * P.inv_dx2;
+            h2[3] = (Lxpyp - Lxpym - Lxmyp + Lxmym) * qq;
+            h2[4] = (Lxpzp - Lxpzm - Lxmzp + Lxmzm) * qq;
+            h2[5] = (Lypzp - Lypzm - Lymzp + Lymzm) * qq;
+#pragma unroll 1
+            for (int t = 1; t < nn; ++t) {
+                const float *ug = M.n111 + (size_t)(P.n111_base + ids[t]) * 24;
+                float un[24];
+                if (P.sym_normals) {
+#pragma unroll
+                    for (int q = 0; q < 12; ++q) un[q] = __ldg(ug + q);
+                    interface_terms<4>(P, G, vL, h2, un, P.use_torque != 0, lap_sl[t], b_sl[t]);
+                } else {
+#pragma unroll
+                    for (int q = 0; q < 24; ++q) un[q] = __ldg(ug + q);
+                    interface_terms<8>(P, G, vL, h2, un, P.use_torque != 0, lap_sl[t], b_sl[t]);
+                }
+            }
+            if (ts > 0) {
+                const Facet fs = facet(gs, M.n111 + (size_t)(P.n111_base + ids[ts]) * 24, P.g2_floor,
+                                       P.sym_normals != 0);
+                const float al = calc_a(P, fs.cabs);
+                w_sl = P.w0 * (al * al);
+            }
+        } else {
+            // isotropic branch of the switchable kernel (:729-731)
+#pragma unroll 1
+            for (int t = 1; t < nn; ++t) {
+                lap_sl[t] = P.eps0sq * lap[0];
+                b_sl[t] = 1.0f;
+            }
+        }
+    } else {
+#pragma unroll 1
+        for (int t = 1; t < nn; ++t) {
+            lap_sl[t] = 0.0f;
+            b_sl[t] = 1.0f;
+        }
+    }
+
+    // Pair sums (:600-661) in O(n^2): for a pair (i, j) the t3 sum of the
+    // reference splits into W_i - W_j (potential) plus either the
+    // solid-liquid term of lap_sl or (A_i - A_j)/2 (gradient energy).
+    const int N = P.N;
+    float W[NA], Ag[NA];
+#pragma unroll 1
+    for (int t1 = 0; t1 < nn; ++t1) {
+        const int i = ids[t1];
+        float w = 0.0f, a = 0.0f;
+#pragma unroll 1
+        for (int t3 = 0; t3 < nn; ++t3) {
+            const int q = ids[t3];
+            const float wik = (q == LIQ && i != LIQ) ? w_sl : __ldg(M.wij + i * N + q);
+            w = fmaf(wik, vc[t3], w);
+            a = fmaf(__ldg(M.a2ij + i * N + q), lap[t3], a);
+        }
+        W[t1] = w;
+        Ag[t1] = a;
+    }
+    const float dT = P.t_uniform ? P.dT_uniform : (float)(M.T0z[k] - P.Tmc);
+    const float inv_n = 1.0f / (float)(n > 0 ? n : 1);
+    float outv[NA];
+#pragma unroll 1
+    for (int t1 = 0; t1 < nn; ++t1) {
+        const int i = ids[t1];
+        float dpi = 0.0f;
+#pragma unroll 1
+        for (int t2 = 0; t2 < nn; ++t2) {
+            if (t2 == t1) continue;
+            const int j = ids[t2];
+            const bool sl = (i != LIQ && j == LIQ), ls = (i == LIQ && j != LIQ);
+            const float T = sl ? 0.5f * lap_sl[t1] : (ls ? -0.5f * lap_sl[t2] : 0.5f * __fsub_rn(Ag[t1], Ag[t2]));
+            const float ppp = __fadd_rn(__fsub_rn(W[t1], W[t2]), T);
+            const float df = sl ? -P.Sf * dT : (ls ? P.Sf * dT : 0.0f);
+            const float tf = __fmul_rn(__fmul_rn(FORCE_PREF, sqrtf(fmaxf(__fmul_rn(vc[t1], vc[t2]), 0.0f))), df);
+            float me = __ldg(M.mij + i * N + j);
+            if (sl) me *= b_sl[t1];
+            else if (ls) me *= b_sl[t2];
+            dpi = __fsub_rn(dpi, __fmul_rn(__fmul_rn(__fmul_rn(2.0f, me), inv_n), __fsub_rn(ppp, tf)));
+        }
+        outv[t1] = fminf(fmaxf(fmaf(P.dt, dpi, vc[t1]), 0.0f), 1.0f);
+    }
+
+    // renormalise with a compensated (TwoSum) float accumulation (:663-680)
+    float sh = 0.0f, sl_ = 0.0f;
+#pragma unroll 1
+    for (int t = 0; t < nn; ++t) {
+        const float a = sh, b = outv[t];
+        const float s2 = a + b;
+        const float bb = s2 - a;
+        sl_ += (a - (s2 - bb)) + (b - bb);
+        sh = s2;
+    }
+    // stored list: the phases that stay positive, ascending
+    int cnt_out = 0, id_first = LIQ;
+    bool sovf = false;
+    const bool normal = sh + sl_ > 1e-20f;
+    float inv = 1.0f / sh;
+    inv = fmaf(-__fmul_rn(inv, inv), sl_, inv);
+    if (!normal) {
+        // all clipped to ~0: the liquid takes the cell (:679-680)
+        out.val[c] = 1.0f;
+        id_first = LIQ;
+        cnt_out = 1;
+    }
+#pragma unroll 1
+    for (int t = 0; t < nn; ++t) {
+        float v;
+        if (normal) {
+            v = outv[t] * inv;
+        } else {
+            if (ids[t] == LIQ) continue;
+            v = outv[t];
+        }
+        if (!(v > 0.0f)) continue;
+        if (cnt_out == S) {
+            sovf = true;
+            continue;
+        }
+        if (cnt_out == 0) id_first = ids[t];
+        else out.idx[(uint32_t)cnt_out * cells + c] = (uint16_t)ids[t];
+        out.val[(uint32_t)cnt_out * cells + c] = v;
+        ++cnt_out;
+    }
+    // one stored phase: its renormalised value is 1 and is left implicit
+    out.head[c] = mkhead(id_first, cnt_out, false);
+    if (sovf) atomicOr(err, MPF3D_DEV_SLOT_OVERFLOW);
+}
+
+// Update of one cell whose neighbourhood is not uniform: the 7-way merge of
+// the neighbour lists, then update_cell over up to AMAX active phases.
 template <int S, int AMAX, bool HEAVY>
 __device__ __forceinline__ void process_cell(const In &in, const Out &out, const Mats &M, const Params &P,
                                              int32_t *__restrict__ err, int l, int m, int k) {
@@ -437,164 +635,7 @@ __device__ __forceinline__ void process_cell(const In &in, const Out &out, const
         }
         return;
     }
-    const int n = A.n;
-    const bool has_liq = n > 0 && A.ids[0] == LIQ;
-    const bool has_solid = n > (has_liq ? 1 : 0);
-    float lap_sl[AMAX], b_sl[AMAX];
-    float w_sl = P.w0;
-    lap_sl[0] = 0.0f;
-    b_sl[0] = 1.0f;
-    if (has_liq && has_solid) {
-        if (HEAVY && P.use_aniso) {
-            // liquid on the 25-point stencil (offsets with |dx|+|dy|+|dz| <= 2)
-            const int lpp = wrap_p(lp, P.nx), lmm = wrap_m(lm, P.nx);
-            const int mpp = wrap_p(mp, P.ny), mmm = wrap_m(mm, P.ny);
-            const int kpp = clamp_p(kp, P.nz), kmm = clamp_m(km, P.nz);
-            const float Lxpyp = liquid32(in, cidx(P, lp, mp, k)), Lxpym = liquid32(in, cidx(P, lp, mm, k));
-            const float Lxmyp = liquid32(in, cidx(P, lm, mp, k)), Lxmym = liquid32(in, cidx(P, lm, mm, k));
-            const float Lxpzp = liquid32(in, cidx(P, lp, m, kp)), Lxpzm = liquid32(in, cidx(P, lp, m, km));
-            const float Lxmzp = liquid32(in, cidx(P, lm, m, kp)), Lxmzm = liquid32(in, cidx(P, lm, m, km));
-            const float Lypzp = liquid32(in, cidx(P, l, mp, kp)), Lypzm = liquid32(in, cidx(P, l, mp, km));
-            const float Lymzp = liquid32(in, cidx(P, l, mm, kp)), Lymzm = liquid32(in, cidx(P, l, mm, km));
-            const float Lx2p = liquid32(in, cidx(P, lpp, m, k)), Lx2m = liquid32(in, cidx(P, lmm, m, k));
-            const float Ly2p = liquid32(in, cidx(P, l, mpp, k)), Ly2m = liquid32(in, cidx(P, l, mmm, k));
-            const float Lz2p = liquid32(in, cidx(P, l, m, kpp)), Lz2m = liquid32(in, cidx(P, l, m, kmm));
-            const float *vL = A.vL;
-            const float g2 = P.inv_2dx;
-            float3 G[7];
-            G[0] = make_float3((vL[1] - vL[2]) * g2, (vL[3] - vL[4]) * g2, (vL[5] - vL[6]) * g2);
-            G[1] = make_float3((Lx2p - vL[0]) * g2, (Lxpyp - Lxpym) * g2, (Lxpzp - Lxpzm) * g2);
-            G[2] = make_float3((vL[0] - Lx2m) * g2, (Lxmyp - Lxmym) * g2, (Lxmzp - Lxmzm) * g2);
-            G[3] = make_float3((Lxpyp - Lxmyp) * g2, (Ly2p - vL[0]) * g2, (Lypzp - Lypzm) * g2);
-            G[4] = make_float3((Lxpym - Lxmym) * g2, (vL[0] - Ly2m) * g2, (Lymzp - Lymzm) * g2);
-            // z neighbours sit on the clamped rows: at the top/bottom row the
-            // neighbour is the cell itself
-            G[5] = (kp == k) ? G[0] : make_float3((Lxpzp - Lxmzp) * g2, (Lypzp - Lymzp) * g2, (Lz2p - vL[0]) * g2);
-            G[6] = (km == k) ? G[0] : make_float3((Lxpzm - Lxmzm) * g2, (Lypzm - Lymzm) * g2, (vL[0] - Lz2m) * g2);
-            if (kp == k) G[5].z = (vL[5] - vL[6]) * g2;
-            if (km == k) G[6].z = (vL[5] - vL[6]) * g2;
-            float h2[6];
-            const float qq = 0.25f * P.inv_dx2;
-            h2[0] = (vL[1] - 2.0f * vL[0] + vL[2]) * P.inv_dx2;
-            h2[1] = (vL[3] - 2.0f * vL[0] + vL[4]) * P.inv_dx2;
-            h2[2] = (vL[5] - 2.0f * vL[0] + vL[6]) * P.inv_dx2;
-            h2[3] = (Lxpyp - Lxpym - Lxmyp + Lxmym) * qq;
-            h2[4] = (Lxpzp - Lxpzm - Lxmzp + Lxmzm) * qq;
-            h2[5] = (Lypzp - Lypzm - Lymzp + Lymzm) * qq;
-            for (int t = 1; t < n; ++t) {
-                const float *ug = M.n111 + (size_t)(P.n111_base + A.ids[t]) * 24;
-                float un[24];
-                if (P.sym_normals) {
-#pragma unroll
-                    for (int q = 0; q < 12; ++q) un[q] = __ldg(ug + q);
-                    interface_terms<4>(P, G, A.vL, h2, un, P.use_torque != 0, lap_sl[t], b_sl[t]);
-                } else {
-#pragma unroll
-                    for (int q = 0; q < 24; ++q) un[q] = __ldg(ug + q);
-                    interface_terms<8>(P, G, A.vL, h2, un, P.use_torque != 0, lap_sl[t], b_sl[t]);
-                }
-            }
-            if (A.ts > 0) {
-                const Facet fs = facet(A.gs, M.n111 + (size_t)(P.n111_base + A.ids[A.ts]) * 24, P.g2_floor,
-                                       P.sym_normals != 0);
-                const float al = calc_a(P, fs.cabs);
-                w_sl = P.w0 * (al * al);
-            }
-        } else {
-            // isotropic branch of the switchable kernel (:729-731)
-            for (int t = 1; t < n; ++t) {
-                lap_sl[t] = P.eps0sq * A.lap[0];
-                b_sl[t] = 1.0f;
-            }
-        }
-    } else {
-        for (int t = 1; t < n; ++t) {
-            lap_sl[t] = 0.0f;
-            b_sl[t] = 1.0f;
-        }
-    }
-
-    // Pair sums (:600-661) in O(n^2): for a pair (i, j) the t3 sum of the
-    // reference splits into W_i - W_j (potential) plus either the
-    // solid-liquid term of lap_sl or (A_i - A_j)/2 (gradient energy).
-    const int N = P.N;
-    float W[AMAX], Ag[AMAX];
-    for (int t1 = 0; t1 < n; ++t1) {
-        const int i = A.ids[t1];
-        float w = 0.0f, a = 0.0f;
-        for (int t3 = 0; t3 < n; ++t3) {
-            const int q = A.ids[t3];
-            const float wik = (q == LIQ && i != LIQ) ? w_sl : __ldg(M.wij + i * N + q);
-            w += wik * A.vc[t3];
-            a += __ldg(M.a2ij + i * N + q) * A.lap[t3];
-        }
-        W[t1] = w;
-        Ag[t1] = a;
-    }
-    const float dT = P.t_uniform ? P.dT_uniform : (float)(M.T0z[k] - P.Tmc);
-    const float inv_n = 1.0f / (float)(n > 0 ? n : 1);
-    float outv[AMAX];
-    for (int t1 = 0; t1 < n; ++t1) {
-        const int i = A.ids[t1];
-        float dpi = 0.0f;
-        for (int t2 = 0; t2 < n; ++t2) {
-            if (t2 == t1) continue;
-            const int j = A.ids[t2];
-            const bool sl = (i != LIQ && j == LIQ), ls = (i == LIQ && j != LIQ);
-            const float T = sl ? 0.5f * lap_sl[t1] : (ls ? -0.5f * lap_sl[t2] : 0.5f * (Ag[t1] - Ag[t2]));
-            const float ppp = (W[t1] - W[t2]) + T;
-            const float df = sl ? -P.Sf * dT : (ls ? P.Sf * dT : 0.0f);
-            const float tf = FORCE_PREF * sqrtf(fmaxf(A.vc[t1] * A.vc[t2], 0.0f)) * df;
-            float me = __ldg(M.mij + i * N + j);
-            if (sl) me *= b_sl[t1];
-            else if (ls) me *= b_sl[t2];
-            dpi -= 2.0f * me * inv_n * (ppp - tf);
-        }
-        outv[t1] = fminf(fmaxf(A.vc[t1] + P.dt * dpi, 0.0f), 1.0f);
-    }
-
-    // renormalise with a compensated (TwoSum) float accumulation (:663-680)
-    float sh = 0.0f, sl_ = 0.0f;
-    for (int t = 0; t < n; ++t) {
-        const float a = sh, b = outv[t];
-        const float s2 = a + b;
-        const float bb = s2 - a;
-        sl_ += (a - (s2 - bb)) + (b - bb);
-        sh = s2;
-    }
-    // stored list: the phases that stay positive, ascending
-    int cnt_out = 0, id_first = LIQ;
-    bool sovf = false;
-    const bool normal = sh + sl_ > 1e-20f;
-    float inv = 1.0f / sh;
-    inv = inv - inv * inv * sl_;
-    if (!normal) {
-        // all clipped to ~0: the liquid takes the cell (:679-680)
-        out.val[c] = 1.0f;
-        id_first = LIQ;
-        cnt_out = 1;
-    }
-    for (int t = 0; t < n; ++t) {
-        float v;
-        if (normal) {
-            v = outv[t] * inv;
-        } else {
-            if (A.ids[t] == LIQ) continue;
-            v = outv[t];
-        }
-        if (!(v > 0.0f)) continue;
-        if (cnt_out == S) {
-            sovf = true;
-            continue;
-        }
-        if (cnt_out == 0) id_first = A.ids[t];
-        else out.idx[(uint32_t)cnt_out * cells + c] = (uint16_t)A.ids[t];
-        out.val[(uint32_t)cnt_out * cells + c] = v;
-        ++cnt_out;
-    }
-    // one stored phase: its renormalised value is 1 and is left implicit
-    out.head[c] = mkhead(id_first, cnt_out, false);
-    if (sovf) atomicOr(err, MPF3D_DEV_SLOT_OVERFLOW);
+    update_cell<S, AMAX, HEAVY>(in, out, M, P, l, m, k, c, A.n, A.ids, A.vc, A.lap, A.vL, A.ts, A.gs, err);
 }
 
 // Kernel 1 of a step: every cell.  Uniform neighbourhoods (the cell and its
@@ -657,6 +698,49 @@ struct BlockSink {
     }
 };
 
+// Classification of cell c = (l, m, k0 + j) from its head h0 and its 6
+// neighbours' heads hn = {x+, x-, y+, y-, z+, z-} (z clamped: a neighbour
+// beyond the domain is the cell itself): a uniform neighbourhood is written
+// directly; any other cell goes to a work list.  Returns whether uniform.
+template <class Sink>
+__device__ __forceinline__ bool sweep_cell(const Out &out, const Params &P, bool split, Sink &sink, int j, uint32_t c,
+                                           uint32_t h0, const uint32_t (&hn)[6]) {
+    bool uniform = hcount(h0) == 1 && !hexplicit(h0);
+    bool liq = hcount(h0) > 0 && hid0(h0) == LIQ;
+    bool sol = hcount(h0) > 1 || (hcount(h0) == 1 && hid0(h0) != LIQ);
+#pragma unroll
+    for (int p = 0; p < 6; ++p) {
+        const uint32_t h = hn[p];
+        uniform = uniform && h == h0;
+        liq = liq || (hcount(h) > 0 && hid0(h) == LIQ);
+        sol = sol || hcount(h) > 1 || (hcount(h) == 1 && hid0(h) != LIQ);
+    }
+    if (uniform) {
+        // the one phase of the neighbourhood keeps the cell at exactly 1
+        out.head[c] = h0;
+        return true;
+    }
+    const bool heavy = liq && sol && P.use_aniso;
+    bool multi = false;
+    if (heavy && split) {
+        // several solids in the active list: a head with 3+ phases or two
+        // solids, or two different solid first ids
+        int sid = -1;
+        const uint32_t hs[7] = {h0, hn[0], hn[1], hn[2], hn[3], hn[4], hn[5]};
+#pragma unroll
+        for (int p = 0; p < 7; ++p) {
+            const int cn = hcount(hs[p]), id = hid0(hs[p]);
+            if (cn >= 3 || (cn == 2 && id != LIQ)) multi = true;
+            else if (cn >= 1 && id != LIQ) {
+                if (sid < 0) sid = id;
+                else if (sid != id) multi = true;
+            }
+        }
+    }
+    sink.add(j, heavy ? (multi ? 2 : 1) : 0, c);
+    return false;
+}
+
 // The sweep of one column of ZB cells (l, m, k0..k0+ZB-1) of a domain;
 // returns whether every one of them was uniform (cells past the top count
 // as uniform).
@@ -691,40 +775,37 @@ __device__ __forceinline__ bool sweep_column(const In &in, const Out &out, const
         // a z neighbour beyond the domain is the cell itself (clamped index)
         if (k == P.nz - 1) hn[4] = h0;
         if (k == 0) hn[5] = h0;
-        bool uniform = hcount(h0) == 1 && !hexplicit(h0);
-        bool liq = hcount(h0) > 0 && hid0(h0) == LIQ;
-        bool sol = hcount(h0) > 1 || (hcount(h0) == 1 && hid0(h0) != LIQ);
+        all_uniform = sweep_cell(out, P, split, sink, j, c, h0, hn) && all_uniform;
+    }
+    return all_uniform;
+}
+
+// The same sweep reading the heads from a shared-memory tile: the block's
+// 32 x by x ZB cells plus a one-cell halo, staged by the Tensor Memory
+// Accelerator (TMA_X columns from l0 - 4, by + 2 rows from m0 - 1, ZB + 2
+// layers from k0 - 1; the periodic x and y halos patched in after the copy).
+constexpr int TMA_X = 40;
+
+template <int ZB, class Sink>
+__device__ __forceinline__ bool sweep_column_tile(const uint32_t *tile, int rows, const Out &out, const Params &P,
+                                                  bool split, Sink &sink, int l, int m, int k0, int l0, int m0) {
+    const uint32_t plane = (uint32_t)P.nx * (uint32_t)P.ny;
+    const uint32_t col = (uint32_t)m * (uint32_t)P.nx + (uint32_t)l;
+    const int xi = l - l0 + 4, yi = m - m0 + 1;
+    auto at = [&](int x, int y, int z) { return tile[(z * rows + y) * TMA_X + x]; };
+    bool all_uniform = true;
 #pragma unroll
-        for (int p = 0; p < 6; ++p) {
-            const uint32_t h = hn[p];
-            uniform = uniform && h == h0;
-            liq = liq || (hcount(h) > 0 && hid0(h) == LIQ);
-            sol = sol || hcount(h) > 1 || (hcount(h) == 1 && hid0(h) != LIQ);
-        }
-        if (uniform) {
-            // the one phase of the neighbourhood keeps the cell at exactly 1
-            out.head[c] = h0;
-        } else {
-            all_uniform = false;
-            const bool heavy = liq && sol && P.use_aniso;
-            bool multi = false;
-            if (heavy && split) {
-                // several solids in the active list: a head with 3+ phases or
-                // two solids, or two different solid first ids
-                int sid = -1;
-                const uint32_t hs[7] = {h0, hn[0], hn[1], hn[2], hn[3], hn[4], hn[5]};
-#pragma unroll
-                for (int p = 0; p < 7; ++p) {
-                    const int cn = hcount(hs[p]), id = hid0(hs[p]);
-                    if (cn >= 3 || (cn == 2 && id != LIQ)) multi = true;
-                    else if (cn >= 1 && id != LIQ) {
-                        if (sid < 0) sid = id;
-                        else if (sid != id) multi = true;
-                    }
-                }
-            }
-            sink.add(j, heavy ? (multi ? 2 : 1) : 0, c);
-        }
+    for (int j = 0; j < ZB; ++j) {
+        const int k = k0 + j;
+        if (k >= P.nz) break;
+        const int zi = j + 1;
+        const uint32_t c = (uint32_t)k * plane + col;
+        const uint32_t h0 = at(xi, yi, zi);
+        uint32_t hn[6] = {at(xi + 1, yi, zi), at(xi - 1, yi, zi), at(xi, yi + 1, zi),
+                          at(xi, yi - 1, zi), at(xi, yi, zi + 1), at(xi, yi, zi - 1)};
+        if (k == P.nz - 1) hn[4] = h0;
+        if (k == 0) hn[5] = h0;
+        all_uniform = sweep_cell(out, P, split, sink, j, c, h0, hn) && all_uniform;
     }
     return all_uniform;
 }
@@ -811,6 +892,162 @@ __global__ void __launch_bounds__(512, 3) sweep_kernel(In in, Out out, Mats M, P
     if (l < P.nx && m < P.ny && k0 < P.nz)
         sink.flush(Q, P.cells32, s_base, (uint32_t)P.nx * (uint32_t)P.ny,
                    P.base + (uint32_t)m * (uint32_t)P.nx + (uint32_t)l, k0);
+}
+
+// Bounded wait on phase `parity` of a shared-memory mbarrier (nanoseconds
+// of %globaltimer); false if it did not complete in time.
+__device__ __forceinline__ bool mbar_wait_ns(uint32_t bar, uint32_t parity, uint64_t limit_ns) {
+    uint64_t t0;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
+    while (true) {
+        uint32_t ok;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.b32 %0, 1, 0, p;\n}\n"
+            : "=r"(ok)
+            : "r"(bar), "r"(parity)
+            : "memory");
+        if (ok) return true;
+        uint64_t t;
+        asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+        if (t - t0 > limit_ns) return false;
+    }
+}
+
+// Kernel 1 with its heads staged in shared memory by one TMA copy per block
+// (cp.async.bulk.tensor.3d of the block's cells plus a one-cell halo from
+// the head array, which the tensor map describes as nx x ny x nz uint32).
+// Blocks whose warps are all quiet copy nothing.  The x and y halos at the
+// domain's periodic edges lie outside the copied box (TMA fills them with
+// zeros) and are patched in with plain loads; z halo layers outside the
+// domain are never read (the clamped neighbour is the cell itself).  A copy
+// that does not land within 1 s sets MPF3D_DEV_STAGING_TIMEOUT and the block
+// waits once more before it leaves.  Same results as sweep_kernel.
+template <int S, int AMAX, int ZB>
+__global__ void __launch_bounds__(512, 3) sweep_kernel_tma(const __grid_constant__ CUtensorMap map, In in, Out out,
+                                                         Params P, Queue Q, int parity, Tiles T,
+                                                         int32_t *__restrict__ err) {
+    constexpr int MAX_ROWS = 16 + 2;
+    __shared__ __align__(128) uint32_t tile[TMA_X * MAX_ROWS * (ZB + 2)];
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ uint32_t s_cnt[3], s_base[3];
+    __shared__ int s_need;
+    const int by = (int)blockDim.y, rows = by + 2;
+    const int l0 = blockIdx.x * 32, m0 = blockIdx.y * by;
+    const int l = l0 + threadIdx.x, m = m0 + threadIdx.y;
+    const int k0 = blockIdx.z * ZB;
+    const int tlin = threadIdx.x + 32 * threadIdx.y;
+    const uint32_t bar_a = (uint32_t)__cvta_generic_to_shared(&bar);
+    if (tlin < 3) s_cnt[tlin] = 0;
+    if (tlin == 0) {
+        s_need = 0;
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar_a) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    if (blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.y == 0 && threadIdx.x < 2)
+        Q.count[2 * (parity ^ 1) + threadIdx.x] = 0;  // the previous step's kernels are done with them
+    if (blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.y == 0 && threadIdx.x == 2 && Q.split)
+        Q.count[4 + (parity ^ 1)] = 0;
+    // quiet flags of this warp's tile (as sweep_kernel)
+    const bool row_ok = m < P.ny && k0 < P.nz;
+    bool quiet = false;
+    uint32_t t = 0;
+    const uint8_t *fin = nullptr;
+    uint8_t *fout = nullptr;
+    if (row_ok && T.flags) {
+        const int tx = (int)blockIdx.x, kb = k0 / ZB;
+        fin = T.flags + (size_t)(parity ^ 1) * T.n;
+        fout = T.flags + (size_t)parity * T.n;
+        auto tid = [&](int a, int b, int c) {
+            return ((uint32_t)c * (uint32_t)P.ny + (uint32_t)b) * (uint32_t)T.ntx + a;
+        };
+        t = tid(tx, m, kb);
+        const uint32_t f0 = fin[t];
+        const uint32_t f1 = fin[tid(tx + 1 < T.ntx ? tx + 1 : 0, m, kb)];
+        const uint32_t f2 = fin[tid(tx > 0 ? tx - 1 : T.ntx - 1, m, kb)];
+        const uint32_t f3 = fin[tid(tx, m + 1 < P.ny ? m + 1 : 0, kb)];
+        const uint32_t f4 = fin[tid(tx, m > 0 ? m - 1 : P.ny - 1, kb)];
+        const uint32_t f5 = fin[tid(tx, m, kb + 1 < T.nkb ? kb + 1 : kb)];
+        const uint32_t f6 = fin[tid(tx, m, kb > 0 ? kb - 1 : kb)];
+        quiet = (f0 & f1 & f2 & f3 & f4 & f5 & f6) != 0u;
+    }
+    __syncthreads();
+    if (row_ok && !quiet && threadIdx.x == 0) s_need = 1;
+    __syncthreads();
+    const bool need = s_need != 0;
+    bool staged = false;
+    if (need) {
+        if (tlin == 0) {
+            const uint32_t bytes = (uint32_t)(TMA_X * rows * (ZB + 2) * 4);
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(bar_a), "r"(bytes)
+                         : "memory");
+            asm volatile(
+                "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+                "[%5];\n" ::"r"((uint32_t)__cvta_generic_to_shared(tile)),
+                "l"(reinterpret_cast<uint64_t>(&map)), "r"(l0 - 4), "r"(m0 - 1), "r"(k0 - 1), "r"(bar_a)
+                : "memory");
+        }
+        staged = mbar_wait_ns(bar_a, 0, 1000000000ull);
+        if (!staged) {
+            if (threadIdx.x == 0) atomicOr(err, MPF3D_DEV_STAGING_TIMEOUT);
+            mbar_wait_ns(bar_a, 0, 1000000000ull);  // the copy may still land: let it, before leaving
+        }
+        staged = __syncthreads_and(staged) != 0;
+        if (staged) {
+            // periodic halos outside the copied box
+            const uint32_t plane = (uint32_t)P.nx * (uint32_t)P.ny;
+            const int nz_box = ZB + 2;
+            if (l0 == 0 || l0 + 32 >= P.nx) {
+                for (int e = tlin; e < 2 * rows * nz_box; e += 32 * by) {
+                    const int side = e / (rows * nz_box), r = e % (rows * nz_box);
+                    const int yi = r % rows, zi = r / rows;
+                    const int gy = m0 - 1 + yi, gz = k0 - 1 + zi;
+                    if (gy < 0 || gy >= P.ny || gz < 0 || gz >= P.nz) continue;
+                    if (side == 0 && l0 == 0)
+                        tile[(zi * rows + yi) * TMA_X + 3] = __ldg(in.head + (uint32_t)gz * plane + (uint32_t)gy * P.nx + (P.nx - 1));
+                    if (side == 1 && l0 + 32 >= P.nx)
+                        tile[(zi * rows + yi) * TMA_X + (P.nx - l0 + 4)] = __ldg(in.head + (uint32_t)gz * plane + (uint32_t)gy * P.nx);
+                }
+            }
+            if (m0 == 0 || m0 + by >= P.ny) {
+                for (int e = tlin; e < 2 * 32 * nz_box; e += 32 * by) {
+                    const int side = e / (32 * nz_box), r = e % (32 * nz_box);
+                    const int xo = r % 32, zi = r / 32;
+                    const int gx = l0 + xo, gz = k0 - 1 + zi;
+                    if (gx >= P.nx || gz < 0 || gz >= P.nz) continue;
+                    if (side == 0 && m0 == 0)
+                        tile[(zi * rows + 0) * TMA_X + xo + 4] = __ldg(in.head + (uint32_t)gz * plane + (uint32_t)(P.ny - 1) * P.nx + gx);
+                    if (side == 1 && m0 + by >= P.ny)
+                        tile[(zi * rows + (P.ny - m0 + 1)) * TMA_X + xo + 4] = __ldg(in.head + (uint32_t)gz * plane + gx);
+                }
+            }
+            __syncthreads();
+        }
+    }
+    BlockSink<ZB> sink(s_cnt);
+    if (row_ok && staged) {
+        if (!T.flags) {
+            if (l < P.nx) sweep_column_tile<ZB>(tile, rows, out, P, Q.split, sink, l, m, k0, l0, m0);
+        } else if (quiet) {
+            if (threadIdx.x == 0) fout[t] = 1;
+        } else {
+            const bool uni = l < P.nx ? sweep_column_tile<ZB>(tile, rows, out, P, Q.split, sink, l, m, k0, l0, m0)
+                                      : true;
+            const bool all = __all_sync(0xffffffffu, uni);
+            if (threadIdx.x == 0) fout[t] = all ? 1 : 0;
+        }
+    } else if (row_ok && quiet && threadIdx.x == 0) {
+        fout[t] = 1;
+    }
+    __syncthreads();
+    if (tlin < 3) {
+        const uint32_t n = s_cnt[tlin];
+        uint32_t *ctr = tlin == 2 ? Q.count + 4 + parity : Q.count + 2 * parity + tlin;
+        s_base[tlin] = n ? atomicAdd(ctr, n) : 0u;
+    }
+    __syncthreads();
+    if (l < P.nx && m < P.ny && k0 < P.nz)
+        sink.flush(Q, P.cells32, s_base, (uint32_t)P.nx * (uint32_t)P.ny, (uint32_t)m * (uint32_t)P.nx + (uint32_t)l,
+                   k0);
 }
 
 // Kernel 2 of a step: the cells queued for the general update, one thread
@@ -1205,15 +1442,51 @@ void launch_side_by_side(cudaStream_t s, bool both, General &&general, Interface
     cudaStreamWaitEvent(s, side.join, 0);  // the caller's stream sees the whole step
 }
 
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link
+// dependency on libcuda)
+PFN_cuTensorMapEncodeTiled_v12000 encode_tiled() {
+    static std::once_flag once;
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    std::call_once(once, [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    });
+    return fn;
+}
+
+// Tensor map of a head array (uint32 nx x ny x nz, x fastest) with boxes of
+// TMA_X x (by + 2) x (zb + 2); out-of-range elements read as zero.  Needs
+// nx a multiple of 4 (16-byte row pitch) and a 16-byte aligned base.
+bool head_map(CUtensorMap *map, const uint32_t *head, int nx, int ny, int nz, int by, int zb) {
+    PFN_cuTensorMapEncodeTiled_v12000 fn = encode_tiled();
+    if (!fn || nx % 4 != 0 || ((uintptr_t)head & 15u) != 0) return false;
+    cuuint64_t dims[3] = {(cuuint64_t)nx, (cuuint64_t)ny, (cuuint64_t)nz};
+    cuuint64_t strides[2] = {(cuuint64_t)nx * 4, (cuuint64_t)nx * ny * 4};
+    cuuint32_t box[3] = {(cuuint32_t)TMA_X, (cuuint32_t)(by + 2), (cuuint32_t)(zb + 2)};
+    cuuint32_t estr[3] = {1u, 1u, 1u};
+    return fn(map, CU_TENSOR_MAP_DATA_TYPE_UINT32, 3, const_cast<uint32_t *>(head), dims, strides, box, estr,
+              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 template <int S, int AMAX>
 void launch_step(const In &in, const Out &out, const Mats &M, const Params &P, const Queue &Q, int parity,
-                 uint8_t *tile_flags, int32_t *err, cudaStream_t s, const mpf3d_tuning &T) {
+                 uint8_t *tile_flags, int32_t *err, cudaStream_t s, const mpf3d_tuning &T, bool sweep_tma) {
     const int by = T.sweep_by;
     dim3 blk(32, by, 1);
+    CUtensorMap map;
+    const bool tma = sweep_tma && P.base == 0 && head_map(&map, in.head, P.nx, P.ny, P.nz, by, T.sweep_zb);
 #define SWEEP_LAUNCH(ZB)                                                                                           \
-    sweep_kernel<S, AMAX, ZB><<<dim3((P.nx + 31) / 32, (P.ny + by - 1) / by, (P.nz + ZB - 1) / ZB), blk, 0, s>>>(    \
-        in, out, M, P, Q, parity,                                                                                  \
-        Tiles{tile_flags, (P.nx + 31) / 32, (P.nz + ZB - 1) / ZB, tiles_of<ZB>(P.nx, P.ny, P.nz)}, err)
+    do {                                                                                                           \
+        const dim3 grid((P.nx + 31) / 32, (P.ny + by - 1) / by, (P.nz + ZB - 1) / ZB);                             \
+        const Tiles tl{tile_flags, (P.nx + 31) / 32, (P.nz + ZB - 1) / ZB, tiles_of<ZB>(P.nx, P.ny, P.nz)};       \
+        if (tma) sweep_kernel_tma<S, AMAX, ZB><<<grid, blk, 0, s>>>(map, in, out, P, Q, parity, tl, err);          \
+        else sweep_kernel<S, AMAX, ZB><<<grid, blk, 0, s>>>(in, out, M, P, Q, parity, tl, err);                    \
+    } while (0)
     if (T.sweep_zb == 2) SWEEP_LAUNCH(2);
     else if (T.sweep_zb == 8) SWEEP_LAUNCH(8);
     else SWEEP_LAUNCH(4);
@@ -1284,6 +1557,18 @@ extern "C" int mpf3d_compact_to_dense(const uint32_t *cnt, const uint16_t *idx, 
     }
 #undef TD
     return cudaGetLastError() == cudaSuccess ? MPF3D_OK : MPF3D_ERR_CUDA;
+}
+
+extern "C" int mpf3d_host_device_pointer(const void *host, void **device) {
+    if (!host || !device) return MPF3D_ERR_ARG;
+    *device = nullptr;
+    void *d = nullptr;
+    if (cudaHostGetDevicePointer(&d, const_cast<void *>(host), 0) != cudaSuccess) {
+        cudaGetLastError();  // not page-locked host memory: clear the error, report it
+        return MPF3D_ERR_ARG;
+    }
+    *device = d;
+    return MPF3D_OK;
 }
 
 extern "C" int mpf3d_compact_active_count(const uint32_t *cnt, const uint16_t *idx, int slots, int nx, int ny, int nz,
@@ -1399,9 +1684,10 @@ extern "C" int mpf3d_compact_step_tuned(const uint32_t *cnt, const uint16_t *idx
     Queue Q{work_items, work_count, (options & MPF3D_STEP_MULTI_LIST) ? 1 : 0};
     parity &= 1;
     cudaStream_t s = (cudaStream_t)stream;
-    if (slots == 4 && amax == 8) launch_step<4, 8>(in, out, M, P, Q, parity, tile_flags, err, s, T);
-    else if (slots == 8 && amax == 16) launch_step<8, 16>(in, out, M, P, Q, parity, tile_flags, err, s, T);
-    else if (slots == 16 && amax == 32) launch_step<16, 32>(in, out, M, P, Q, parity, tile_flags, err, s, T);
+    const bool tma = (options & MPF3D_STEP_SWEEP_TMA) != 0;
+    if (slots == 4 && amax == 8) launch_step<4, 8>(in, out, M, P, Q, parity, tile_flags, err, s, T, tma);
+    else if (slots == 8 && amax == 16) launch_step<8, 16>(in, out, M, P, Q, parity, tile_flags, err, s, T, tma);
+    else if (slots == 16 && amax == 32) launch_step<16, 32>(in, out, M, P, Q, parity, tile_flags, err, s, T, tma);
     else return MPF3D_ERR_ARG;
     return cudaGetLastError() == cudaSuccess ? MPF3D_OK : MPF3D_ERR_CUDA;
 }

@@ -13,6 +13,7 @@ LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libmpf3d.so
 
 MPF3D_OK = 0
 STEP_MULTI_LIST = 1  # MPF3D_STEP_MULTI_LIST
+STEP_SWEEP_TMA = 2  # MPF3D_STEP_SWEEP_TMA
 ERRORS = {-1: "bad argument", -2: "bad dtype", -3: "CUDA launch/call failed", -4: "size above limit"}
 
 DEV_BITS = {1: "unchecked APT needed more rows than mf has (MPF3D_DEV_MF_DEPTH)",
@@ -20,7 +21,8 @@ DEV_BITS = {1: "unchecked APT needed more rows than mf has (MPF3D_DEV_MF_DEPTH)"
             4: "update met an mf id outside [0, N) (MPF3D_DEV_BAD_ID)",
             8: "compact stepper: more phases than slots (MPF3D_DEV_SLOT_OVERFLOW)",
             16: "compact conversion met a negative or NaN phi (MPF3D_DEV_BAD_INPUT)",
-            32: "tcgen05 GEMM: a bounded wait ran out, outputs written as NaN (MPF3D_DEV_GEMM_ABORT)"}
+            32: "tcgen05 GEMM: a bounded wait ran out, outputs written as NaN (MPF3D_DEV_GEMM_ABORT)",
+            64: "compact step: a TMA staging copy did not land in time (MPF3D_DEV_STAGING_TIMEOUT)"}
 
 _VP = ctypes.c_void_p
 _I32 = ctypes.c_int
@@ -53,6 +55,7 @@ _U32 = ctypes.c_uint32
 
 # name -> (restype, argtypes)
 _SIGS = {
+    "mpf3d_host_device_pointer": (_I32, [_VP, ctypes.POINTER(ctypes.c_void_p)]),
     "mpf3d_version": (_I32, []),
     "mpf3d_dense_apt": (_I32, [_VP, _I32, _I32, _I32, _I32, _I32, _VP, _I32, _VP, _VP, _I32, _VP, _VP]),
     "mpf3d_dense_update": (_I32, [_VP, _VP, _I32, _VP, _I32, _VP, _I32, _VP, _VP, _VP, _VP, _VP,
@@ -153,3 +156,11 @@ def check(rc: int, what: str) -> None:
 
 def describe_dev_error(word: int) -> str:
     return "; ".join(msg for bit, msg in DEV_BITS.items() if word & bit) or "none"
+
+
+def host_device_pointer(t) -> int:
+    """Device address of a pinned (page-locked) CPU tensor's memory, so that a
+    kernel can read or write it over the CPU-GPU link without a staging copy."""
+    d = ctypes.c_void_p()
+    check(lib().mpf3d_host_device_pointer(t.data_ptr(), ctypes.byref(d)), "host_device_pointer")
+    return int(d.value)

@@ -2,8 +2,9 @@
 
 The reference launches every kernel with a fixed [4, 4, 4] block
 (config_3d.yaml gpu.threads_per_block).  Here the shape -- cells per sweep
-thread along z, sweep block height, and the grid and block sizes of the two
-work-list kernels -- is searched per problem (grid, phases, slots, model
+thread along z, sweep block height, the grid and block sizes of the two
+work-list kernels, and whether the sweep stages its heads in shared memory by
+TMA -- is searched per problem (grid, phases, slots, model
 switches, GPU) by timing each candidate on the solver's own state with CUDA
 events, restoring the state before every trial.  All shapes compute identical
 results.  Winners are cached in a JSON file (MPF3D_TUNING_CACHE, default
@@ -61,15 +62,16 @@ def _store(db: dict) -> None:
     os.replace(tmp, p)
 
 
-def time_config(solver, cfg, steps: int) -> float:
-    """Milliseconds per step of `cfg` on the solver's current state (restored
-    afterwards)."""
+def time_config(solver, cfg, steps: int, sweep_tma: bool = False) -> float:
+    """Milliseconds per step of `cfg` (and the sweep form) on the solver's
+    current state (restored afterwards)."""
     import torch
 
     snap = [t.clone() for t in solver.buf[solver.cur]]
     cur, count = solver.cur, solver.step_count
-    prev = solver.tuning
+    prev, prev_tma = solver.tuning, solver.sweep_tma
     solver.tuning = make(cfg)
+    solver.sweep_tma = sweep_tma
     solver.forget_history()  # the trial starts from the snapshot, not from the last step
     stream = torch.cuda.current_stream(solver.device)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -82,7 +84,7 @@ def time_config(solver, cfg, steps: int) -> float:
         torch.cuda.synchronize(solver.device)
         ms = e0.elapsed_time(e1) / steps
     finally:
-        solver.tuning = prev
+        solver.tuning, solver.sweep_tma = prev, prev_tma
         solver.cur, solver.step_count = cur, count
         for dst, src in zip(solver.buf[cur], snap):
             dst.copy_(src)
@@ -97,6 +99,7 @@ def tune(solver, steps: int = 8, use_cache: bool = True) -> dict:
     db = _load() if use_cache else {}
     if use_cache and key in db:
         solver.tuning = make(db[key]["config"])
+        solver.sweep_tma = bool(db[key].get("sweep_tma", False))
         return db[key]
     trials = {}
     base = time_config(solver, DEFAULT, steps)
@@ -116,8 +119,17 @@ def tune(solver, steps: int = 8, use_cache: bool = True) -> dict:
             trials[str(cfg)] = time_config(solver, cfg, steps)
         if trials[str(cfg)] < best_ms:
             best, best_ms = cfg, trials[str(cfg)]
+    # stage 3: the sweep with its heads staged in shared memory by TMA
+    tma = False
+    if solver.nx % 4 == 0:
+        ms = time_config(solver, best, steps, sweep_tma=True)
+        trials[str(best) + " tma"] = ms
+        if ms < best_ms:
+            tma, best_ms = True, ms
     solver.tuning = make(best)
-    rec = {"config": list(best), "ms_per_step": best_ms, "default_ms_per_step": base, "trials": trials}
+    solver.sweep_tma = tma
+    rec = {"config": list(best), "sweep_tma": tma, "ms_per_step": best_ms, "default_ms_per_step": base,
+           "trials": trials}
     if use_cache:
         db[key] = rec
         _store(db)

@@ -105,6 +105,10 @@ class CompactSolver:
                                                      self.nz, self.slots, h.data_ptr(), i_.data_ptr(),
                                                      v.data_ptr(), self._stream())
             _lib.check(rc, "compact_init_owner")
+        elif phi.device.type == "cpu" and phi.is_pinned() and phi.is_contiguous():
+            # pinned host memory: the converter reads it in place over the
+            # CPU-GPU link (no device copy of the dense field)
+            self._from_dense(phi, _lib.host_device_pointer(phi))
         else:
             dphi = phi.to(self.device).contiguous()
             self._from_dense(dphi)
@@ -141,6 +145,8 @@ class CompactSolver:
         self.tuning = None  # launch shape (mpf3d_tuning); None = library default
         # quiet-tile flags of the sweep (see mpf3d_compact_step_tuned)
         self.skip_quiet_tiles = True
+        # the sweep stages its heads in shared memory by TMA (same results)
+        self.sweep_tma = False
         n_flags = int(_lib.lib().mpf3d_compact_tile_flags_len(self.nx, self.ny, self.nz))
         self.tile_flags = torch.zeros(max(n_flags, 1), dtype=torch.uint8, device=self.device)
         self._tiles_zb = None
@@ -178,11 +184,11 @@ class CompactSolver:
     def _stream(self):
         return _torch().cuda.current_stream(self.device).cuda_stream or None
 
-    def _from_dense(self, dphi):
+    def _from_dense(self, dphi, ptr=None):
         torch = _torch()
         cnt, idx, val = self.buf[self.cur]
         rc = _lib.lib().mpf3d_compact_from_dense(
-            dphi.data_ptr(), 0 if dphi.dtype == torch.float32 else 1, self.N, self.nx, self.ny,
+            dphi.data_ptr() if ptr is None else ptr, 0 if dphi.dtype == torch.float32 else 1, self.N, self.nx, self.ny,
             self.nz, self.slots, cnt.data_ptr(), idx.data_ptr(), val.data_ptr(),
             self.err.data_ptr(), self._stream())
         _lib.check(rc, "compact_from_dense")
@@ -211,7 +217,8 @@ class CompactSolver:
             int(self.torque), int(self.symmetric_normals), self.work_items.data_ptr(),
             self.work_count.data_ptr(), step_index & 1, self.err.data_ptr(), self._stream(),
             ctypes.byref(self.tuning) if self.tuning is not None else None,
-            self.tile_flags.data_ptr() if self.skip_quiet_tiles else None, _lib.STEP_MULTI_LIST)
+            self.tile_flags.data_ptr() if self.skip_quiet_tiles else None,
+            _lib.STEP_MULTI_LIST | (_lib.STEP_SWEEP_TMA if self.sweep_tma else 0))
         _lib.check(rc, "compact_step")
         self.cur = 1 - self.cur
 
@@ -271,16 +278,35 @@ class CompactSolver:
             raise RuntimeError(f"compact solver device error: {msg}")
 
     # -- outputs ----------------------------------------------------------------
-    def to_dense(self, dtype=np.float32, host: bool = True):
+    def to_dense(self, dtype=np.float32, host: bool = True, out=None):
+        """Dense phi [N, nx, ny, nz].  With `out` (a contiguous tensor of that
+        shape and of dtype float32 or float64) the field is written there
+        and `out` is returned: a pinned CPU tensor is written in place over
+        the CPU-GPU link, asynchronously on the solver's stream (synchronise
+        before reading it)."""
         torch = _torch()
-        tdt = torch.float32 if np.dtype(dtype) == np.float32 else torch.float64
-        out = torch.empty((self.N, self.nx, self.ny, self.nz), dtype=tdt, device=self.device)
+        shape = (self.N, self.nx, self.ny, self.nz)
+        if out is not None:
+            if tuple(out.shape) != shape or out.dtype not in (torch.float32, torch.float64) or not out.is_contiguous():
+                raise ValueError(f"out must be a contiguous float32/float64 tensor of shape {shape}")
+            tdt = out.dtype
+            if out.device.type == "cpu":
+                if not out.is_pinned():
+                    raise ValueError("a CPU `out` must be pinned (page-locked)")
+                ptr = _lib.host_device_pointer(out)
+            else:
+                ptr = out.data_ptr()
+        else:
+            tdt = torch.float32 if np.dtype(dtype) == np.float32 else torch.float64
+            out = torch.empty(shape, dtype=tdt, device=self.device)
+            ptr = out.data_ptr()
         cnt, idx, val = self.buf[self.cur]
         rc = _lib.lib().mpf3d_compact_to_dense(cnt.data_ptr(), idx.data_ptr(), val.data_ptr(),
                                                self.slots, self.N, self.nx, self.ny, self.nz,
-                                               out.data_ptr(), 0 if tdt == torch.float32 else 1,
-                                               self._stream())
+                                               ptr, 0 if tdt == torch.float32 else 1, self._stream())
         _lib.check(rc, "compact_to_dense")
+        if out.device.type == "cpu":
+            return out
         return out.cpu().numpy() if host else out
 
     def active_count(self, host: bool = True):

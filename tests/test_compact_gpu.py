@@ -196,3 +196,50 @@ def test_two_stream_step_replays_from_a_cuda_graph():
     assert np.array_equal(a.to_dense(), b.to_dense())
     a.check()
     b.check()
+
+
+def test_pinned_host_conversion_in_place():
+    """Dense phi in pinned host memory is converted in place over the CPU-GPU
+    link (no device copy) and written back in place: the state and the
+    written field equal those of the device-memory path."""
+    from mpf3d import inputs
+    case = inputs.voronoi_case(40, 24, 36, 7, 10, seed=12, orientation_seed=1)
+    pinned = torch.from_numpy(case.phi).pin_memory()
+    a = make_solver(case)
+    from mpf3d.solver import CompactSolver
+    b = CompactSolver(pinned, case.temp, case.n111, case.wij, case.aij, case.mij, case.phys)
+    assert np.array_equal(a.to_dense(), b.to_dense())
+    a.step(3)
+    b.step(3)
+    out = torch.empty(case.phi.shape, dtype=torch.float32).pin_memory()
+    out.fill_(-1.0)
+    r = b.to_dense(out=out)
+    torch.cuda.synchronize()
+    assert r is out
+    assert np.array_equal(out.numpy(), a.to_dense())
+    with pytest.raises(ValueError):
+        b.to_dense(out=torch.empty(case.phi.shape, dtype=torch.float32))  # not pinned
+
+
+@pytest.mark.parametrize("shape,cfg", [((72, 20, 64), None), ((36, 13, 30), (8, 4, 8, 256, 8, 128)),
+                                       ((64, 24, 40), (2, 16, 32, 128, 32, 64))])
+def test_tma_staged_sweep_changes_nothing(shape, cfg):
+    """The sweep with each block's heads staged in shared memory by one TMA
+    copy (periodic x/y halos patched in, clamped z) classifies exactly like
+    the plain sweep: the states agree bit for bit over a moving front with
+    quiet tiles, on domains whose x and y extents are not multiples of the
+    block (partial edge tiles)."""
+    from mpf3d import autotune, inputs
+    nx, ny, nz = shape
+    case = inputs.voronoi_case(nx, ny, nz, 6, 10, seed=21, orientation_seed=3, undercooling=1.5)
+    a = make_solver(case)
+    b = make_solver(case)
+    b.sweep_tma = True
+    if cfg is not None:
+        a.tuning = autotune.make(cfg)
+        b.tuning = autotune.make(cfg)
+    for chunk in range(4):
+        a.step(8)
+        b.step(8)
+        assert np.array_equal(a.to_dense(), b.to_dense()), f"after {8 * (chunk + 1)} steps"
+    b.check()
