@@ -781,10 +781,13 @@ def bicrystal_run(args, dev, rank=0, world=1):
     dims, q, dT, da = dims_all[lo:hi], q_all[lo:hi], dT_all[lo:hi], da_all[lo:hi]
     n = hi - lo
     b = BatchedBicrystals(dims, q, dT, da, base_height=16.0, slots=4, device=dev)
+    tuned = b.autotune(steps=8) if not args.no_autotune else None
     b.capture(50)
     b.step(50)  # warm-up replay
     torch.cuda.synchronize(dev)
+    tuning = b.tuning
     b = BatchedBicrystals(dims, q, dT, da, base_height=16.0, slots=4, device=dev)
+    b.tuning = tuning
     b.capture(50)
     torch.cuda.synchronize(dev)
     t0 = time.perf_counter()
@@ -811,7 +814,9 @@ def bicrystal_run(args, dev, rank=0, world=1):
             "gb_inclination_deg": {"finite": int(np.isfinite(ang).sum()),
                                    "median_abs": float(np.nanmedian(np.abs(ang))) if np.isfinite(ang).any()
                                    else None},
-            "launches_per_step": 3, "graph_steps": 50}
+            "launches_per_step": 3, "graph_steps": 50,
+            "launch_shape": {"work_list_kernels": list(tuned["config"][2:]), "ms_per_step_tuned": tuned["ms_per_step"],
+                             "ms_per_step_default": tuned["default_ms_per_step"]} if tuned else None}
 
 
 def emit(args, rank, world, value, ms, cells, t_e2e, in_bytes, out_bytes, achieved, peak, peak_kind,

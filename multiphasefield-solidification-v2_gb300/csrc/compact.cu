@@ -1637,15 +1637,22 @@ Params shared_params(const mpf3d_scalars *sc, int enable_anisotropy, int enable_
 
 template <int S, int AMAX>
 void launch_batched(const In &in, const Out &out, const Mats &M, const Params &P0, const mpf3d_instance *inst,
-                    int n_inst, int n_tiles, const Queue &Q, int parity, int32_t *err, cudaStream_t s) {
+                    int n_inst, int n_tiles, const Queue &Q, int parity, int32_t *err, cudaStream_t s,
+                    const mpf3d_tuning &T) {
     batched_sweep_kernel<S, AMAX><<<n_tiles, dim3(32, 8, 1), 0, s>>>(in, out, P0, inst, n_inst, Q, parity);
-    // one stream: the batch's fixed queue grids already fill the SMs, and the
-    // side-by-side launch of the compact step measured no gain here
+    // one stream: the side-by-side launch of the compact step measured no
+    // gain here; the work-list grids come from T (the sweep's 32 x 8 x 4
+    // tiles are fixed by the instance table)
     const int sms = sms_of_current_device();
-    batched_queue_kernel<S, AMAX, false><<<sms * 8, 256, 0, s>>>(in, out, M, P0, inst, n_inst, Q, parity, err);
+    batched_queue_kernel<S, AMAX, false><<<sms * T.general_blocks_per_sm, T.general_threads, 0, s>>>(
+        in, out, M, P0, inst, n_inst, Q, parity, err);
     if (P0.use_aniso)
-        batched_queue_kernel<S, AMAX, true><<<sms * 8, 128, 0, s>>>(in, out, M, P0, inst, n_inst, Q, parity, err);
+        batched_queue_kernel<S, AMAX, true><<<sms * T.iface_blocks_per_sm, T.iface_threads, 0, s>>>(
+            in, out, M, P0, inst, n_inst, Q, parity, err);
 }
+
+// launch shape of the batched step before it was tuned
+const mpf3d_tuning kBatchedDefault = {4, 8, 8, 256, 8, 128};
 
 }  // namespace
 
@@ -1746,13 +1753,15 @@ extern "C" int mpf3d_batched_init_bicrystal(const mpf3d_instance *inst, int n_in
     return cudaGetLastError() == cudaSuccess ? MPF3D_OK : MPF3D_ERR_CUDA;
 }
 
-extern "C" int mpf3d_batched_step(const uint32_t *head, const uint16_t *idx, const float *val, uint32_t *head_out,
-                                  uint16_t *idx_out, float *val_out, int slots, int amax, const mpf3d_instance *inst,
-                                  int n_inst, int n_tiles, uint32_t total_cells, const float *wij, const float *a2ij,
-                                  const float *mij, const float *n111, int N, const mpf3d_scalars *sc,
-                                  int enable_anisotropy, int enable_torque, int symmetric_normals,
-                                  uint32_t *work_items, uint32_t *work_count, int parity, int32_t *err,
-                                  void *stream, int options) {
+extern "C" int mpf3d_batched_step_tuned(const uint32_t *head, const uint16_t *idx, const float *val,
+                                        uint32_t *head_out, uint16_t *idx_out, float *val_out, int slots, int amax,
+                                        const mpf3d_instance *inst, int n_inst, int n_tiles, uint32_t total_cells,
+                                        const float *wij, const float *a2ij, const float *mij, const float *n111, int N,
+                                        const mpf3d_scalars *sc, int enable_anisotropy, int enable_torque,
+                                        int symmetric_normals, uint32_t *work_items, uint32_t *work_count, int parity,
+                                        int32_t *err, void *stream, int options, const mpf3d_tuning *tuning) {
+    const mpf3d_tuning T = tuning ? *tuning : kBatchedDefault;
+    if (!tuning_ok(T)) return MPF3D_ERR_ARG;
     if (!head || !idx || !val || !head_out || !idx_out || !val_out || !inst || !wij || !a2ij || !mij || !n111 ||
         !sc || !err || !work_items || !work_count || n_inst <= 0 || n_tiles <= 0 || total_cells == 0 || N <= 0 ||
         N > 65535)
@@ -1769,11 +1778,24 @@ extern "C" int mpf3d_batched_step(const uint32_t *head, const uint16_t *idx, con
     Queue Q{work_items, work_count, (options & MPF3D_STEP_MULTI_LIST) ? 1 : 0};
     cudaStream_t s = (cudaStream_t)stream;
     parity &= 1;
-    if (slots == 4 && amax == 8) launch_batched<4, 8>(in, out, M, P0, inst, n_inst, n_tiles, Q, parity, err, s);
-    else if (slots == 8 && amax == 16) launch_batched<8, 16>(in, out, M, P0, inst, n_inst, n_tiles, Q, parity, err, s);
-    else if (slots == 16 && amax == 32) launch_batched<16, 32>(in, out, M, P0, inst, n_inst, n_tiles, Q, parity, err, s);
+    if (slots == 4 && amax == 8) launch_batched<4, 8>(in, out, M, P0, inst, n_inst, n_tiles, Q, parity, err, s, T);
+    else if (slots == 8 && amax == 16) launch_batched<8, 16>(in, out, M, P0, inst, n_inst, n_tiles, Q, parity, err, s, T);
+    else if (slots == 16 && amax == 32) launch_batched<16, 32>(in, out, M, P0, inst, n_inst, n_tiles, Q, parity, err, s, T);
     else return MPF3D_ERR_ARG;
     return cudaGetLastError() == cudaSuccess ? MPF3D_OK : MPF3D_ERR_CUDA;
+}
+
+extern "C" int mpf3d_batched_step(const uint32_t *head, const uint16_t *idx, const float *val, uint32_t *head_out,
+                                  uint16_t *idx_out, float *val_out, int slots, int amax, const mpf3d_instance *inst,
+                                  int n_inst, int n_tiles, uint32_t total_cells, const float *wij, const float *a2ij,
+                                  const float *mij, const float *n111, int N, const mpf3d_scalars *sc,
+                                  int enable_anisotropy, int enable_torque, int symmetric_normals,
+                                  uint32_t *work_items, uint32_t *work_count, int parity, int32_t *err,
+                                  void *stream, int options) {
+    return mpf3d_batched_step_tuned(head, idx, val, head_out, idx_out, val_out, slots, amax, inst, n_inst, n_tiles,
+                                    total_cells, wij, a2ij, mij, n111, N, sc, enable_anisotropy, enable_torque,
+                                    symmetric_normals, work_items, work_count, parity, err, stream, options,
+                                    nullptr);
 }
 
 extern "C" int mpf3d_batched_fronts(const uint32_t *head, const uint16_t *idx, const float *val, int slots,

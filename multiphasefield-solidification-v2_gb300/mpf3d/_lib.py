@@ -87,6 +87,9 @@ _SIGS = {
     "mpf3d_batched_step": (_I32, [_VP, _VP, _VP, _VP, _VP, _VP, _I32, _I32, _VP, _I32, _I32, ctypes.c_uint32,
                                   _VP, _VP, _VP, _VP, _I32, ctypes.POINTER(Scalars), _I32, _I32, _I32, _VP,
                                   _VP, _I32, _VP, _VP, _I32]),
+    "mpf3d_batched_step_tuned": (_I32, [_VP, _VP, _VP, _VP, _VP, _VP, _I32, _I32, _VP, _I32, _I32, ctypes.c_uint32,
+                                        _VP, _VP, _VP, _VP, _I32, ctypes.POINTER(Scalars), _I32, _I32, _I32, _VP,
+                                        _VP, _I32, _VP, _VP, _I32, _VP]),
     "mpf3d_batched_fronts": (_I32, [_VP, _VP, _VP, _I32, _VP, _I32, ctypes.c_uint32, _VP, _VP]),
     "mpf3d_batched_gb_rows": (_I32, [_VP, _VP, _VP, _I32, _VP, _I32, ctypes.c_uint32, _VP, _VP, _VP]),
     "mpf3d_compact_init_owner": (_I32, [_VP, _I32, _VP, _I32, _I32, _I32, _I32, _VP, _VP, _VP, _VP]),

@@ -134,3 +134,60 @@ def tune(solver, steps: int = 8, use_cache: bool = True) -> dict:
         db[key] = rec
         _store(db)
     return rec
+
+
+def tune_batched(batch, steps: int = 8, use_cache: bool = True) -> dict:
+    """Search the grid and block sizes of the batched step's two work-list
+    kernels (the QUEUE candidates) on the batch's own state, restored after
+    every trial; sets batch.tuning.  Cached per (GPU, instance count, total
+    cells, slots, model switches)."""
+    import torch
+
+    name = torch.cuda.get_device_name(batch.device)
+    key = (f"batched|{name}|n{batch.n}|cells{batch.total_cells}|S{batch.slots}|"
+           f"a{int(batch.anisotropy)}t{int(batch.torque)}")
+    db = _load() if use_cache else {}
+    if use_cache and key in db:
+        batch.tuning = make(db[key]["config"])
+        return db[key]
+    if batch.graph is not None:
+        raise RuntimeError("tune the batch before capturing a graph of its steps")
+
+    def trial(cfg):
+        snap = [t.clone() for t in batch.buf[batch.cur]]
+        cur, count = batch.cur, batch.step_count
+        prev = batch.tuning
+        batch.tuning = make(cfg)
+        stream = torch.cuda.current_stream(batch.device)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        try:
+            batch.launch_step()
+            e0.record(stream)
+            for _ in range(steps):
+                batch.launch_step()
+            e1.record(stream)
+            torch.cuda.synchronize(batch.device)
+            return e0.elapsed_time(e1) / steps
+        finally:
+            batch.tuning = prev
+            batch.cur, batch.step_count = cur, count
+            for dst, src in zip(batch.buf[cur], snap):
+                dst.copy_(src)
+            batch.work_count.zero_()
+
+    trials = {}
+    base = trial(DEFAULT)
+    trials[str(DEFAULT)] = base
+    best, best_ms = DEFAULT, base
+    for q in QUEUE:
+        cfg = DEFAULT[:2] + q
+        if str(cfg) not in trials:
+            trials[str(cfg)] = trial(cfg)
+        if trials[str(cfg)] < best_ms:
+            best, best_ms = cfg, trials[str(cfg)]
+    batch.tuning = make(best)
+    rec = {"config": list(best), "ms_per_step": best_ms, "default_ms_per_step": base, "trials": trials}
+    if use_cache:
+        db[key] = rec
+        _store(db)
+    return rec

@@ -125,6 +125,7 @@ class BatchedBicrystals:
         self.cur = 0
         self.step_count = 0
         self.graph = None
+        self.tuning = None  # work-list kernel shape (mpf3d_tuning); None = library default
         h, i_, v = self.buf[0]
         self.layout = layout
         if layout == "bicrystal":
@@ -176,15 +177,23 @@ class BatchedBicrystals:
     def launch_step(self) -> None:
         src, dst = self.buf[self.cur], self.buf[1 - self.cur]
         self.step_count += 1
-        rc = _lib.lib().mpf3d_batched_step(
+        rc = _lib.lib().mpf3d_batched_step_tuned(
             src[0].data_ptr(), src[1].data_ptr(), src[2].data_ptr(), dst[0].data_ptr(), dst[1].data_ptr(),
             dst[2].data_ptr(), self.slots, self.amax, self._ip(), self.n, self.n_tiles, self.total_cells,
             self.wij.data_ptr(), self.a2ij.data_ptr(), self.mij.data_ptr(), self.n111.data_ptr(), 3,
             ctypes.byref(self.scalars), int(self.anisotropy), int(self.torque), int(self.symmetric_normals),
             self.work_items.data_ptr(), self.work_count.data_ptr(), self.step_count & 1,
-            self.err.data_ptr(), self._stream(), _lib.STEP_MULTI_LIST)
+            self.err.data_ptr(), self._stream(), _lib.STEP_MULTI_LIST,
+            ctypes.byref(self.tuning) if self.tuning is not None else None)
         _lib.check(rc, "batched_step")
         self.cur = 1 - self.cur
+
+    def autotune(self, steps: int = 8, use_cache: bool = True) -> dict:
+        """Pick the fastest work-list kernel shape for this batch (see
+        mpf3d.autotune.tune_batched); call before capture()."""
+        from . import autotune
+
+        return autotune.tune_batched(self, steps=steps, use_cache=use_cache)
 
     def capture(self, steps: int):
         """Capture `steps` (even) consecutive steps in a CUDA graph."""

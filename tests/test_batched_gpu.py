@@ -72,3 +72,28 @@ def test_observables_match_host_reductions():
         assert math.isclose(v2[i], phi[2].sum(), rel_tol=1e-6)
     ang = b.gb_inclination(z_from=0)
     assert np.all(np.isfinite(ang)) and np.all(np.abs(ang) < 45.0)
+
+
+def test_every_work_list_shape_gives_the_same_batch(tmp_path, monkeypatch):
+    """The batched step's work-list kernel shapes (the autotuner's candidates)
+    only reschedule the work: results bit identical; the tuner restores the
+    state it timed on and caches its pick."""
+    from mpf3d import autotune
+    monkeypatch.setenv("MPF3D_TUNING_CACHE", str(tmp_path / "tuning.json"))
+    ref, _ = make_batch()
+    ref.step(6, use_graph=False)
+    for cfg in [(4, 8, 4, 256, 4, 128), (4, 8, 32, 128, 32, 64), (4, 8, 16, 128, 16, 64)]:
+        b, _ = make_batch()
+        b.tuning = autotune.make(cfg)
+        b.step(6, use_graph=False)
+        for i in range(len(DIMS)):
+            assert np.array_equal(b.dense(i), ref.dense(i)), cfg
+    b, _ = make_batch()
+    before = [b.dense(i) for i in range(len(DIMS))]
+    rec = b.autotune(steps=2)
+    assert all(np.array_equal(b.dense(i), before[i]) for i in range(len(DIMS)))
+    assert rec["ms_per_step"] <= rec["default_ms_per_step"]
+    b.step(6, use_graph=False)
+    for i in range(len(DIMS)):
+        assert np.array_equal(b.dense(i), ref.dense(i))
+    assert (tmp_path / "tuning.json").exists()
