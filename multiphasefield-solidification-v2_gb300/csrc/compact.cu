@@ -706,19 +706,20 @@ template <class Sink>
 __device__ __forceinline__ bool sweep_cell(const Out &out, const Params &P, bool split, Sink &sink, int j, uint32_t c,
                                            uint32_t h0, const uint32_t (&hn)[6]) {
     bool uniform = hcount(h0) == 1 && !hexplicit(h0);
+#pragma unroll
+    for (int p = 0; p < 6; ++p) uniform = uniform && hn[p] == h0;
+    if (uniform) {
+        // the one phase of the neighbourhood keeps the cell at exactly 1
+        out.head[c] = h0;
+        return true;
+    }
     bool liq = hcount(h0) > 0 && hid0(h0) == LIQ;
     bool sol = hcount(h0) > 1 || (hcount(h0) == 1 && hid0(h0) != LIQ);
 #pragma unroll
     for (int p = 0; p < 6; ++p) {
         const uint32_t h = hn[p];
-        uniform = uniform && h == h0;
         liq = liq || (hcount(h) > 0 && hid0(h) == LIQ);
         sol = sol || hcount(h) > 1 || (hcount(h) == 1 && hid0(h) != LIQ);
-    }
-    if (uniform) {
-        // the one phase of the neighbourhood keeps the cell at exactly 1
-        out.head[c] = h0;
-        return true;
     }
     const bool heavy = liq && sol && P.use_aniso;
     bool multi = false;
