@@ -100,14 +100,10 @@ __device__ __forceinline__ Facet facet_n(float3 g, const float *__restrict__ u, 
     return f;
 }
 
-__device__ __forceinline__ Facet facet(float3 g, const float *__restrict__ u, float g2_floor, bool sym) {
-    return sym ? facet_n<4>(g, u, g2_floor) : facet_n<8>(g, u, g2_floor);
-}
-
 // facet_n over normals already held in registers (a grain's normals are
 // loaded once per cell and reused at the 7 stencil points)
 template <int NT>
-__device__ __forceinline__ Facet facet_regs(float3 g, const float (&u)[24], float g2_floor) {
+__device__ __forceinline__ Facet facet_regs(float3 g, const float (&u)[3 * NT], float g2_floor) {
     Facet f;
     f.q = g.x * g.x + g.y * g.y + g.z * g.z;
     f.valid = !(f.q < g2_floor);
@@ -368,7 +364,7 @@ __device__ __forceinline__ PointTerms point_terms(const Params &P, float3 g, con
 // :386-441, A13_divergence_3d :344-383, calc_b_from_cos :33-55).
 template <int NT>
 __device__ __forceinline__ void interface_terms(const Params &P, const float3 (&G)[7], const float (&vL)[7],
-                                                const float (&h2)[6], const float (&u)[24], bool torque,
+                                                const float (&h2)[6], const float (&u)[3 * NT], bool torque,
                                                 float &lap_sl, float &b_sl) {
     Facet F[7];
     bool any = false;
@@ -431,9 +427,12 @@ __device__ __forceinline__ void interface_terms(const Params &P, const float3 (&
 // ids (ascending), values vc and Laplacians lap of the n active phases, the
 // liquid at the 7 points, and the dominant solid ts (index, -1 if none) with
 // its gradient gs.  HEAVY enables the anisotropic solid-liquid terms (cells
-// with liquid and a solid active).  The per-phase loops are kept rolled:
-// unrolled copies of this body made the kernels wait on instruction fetch.
-template <int S, int NA, bool HEAVY>
+// with liquid and a solid active) with NT normals per grain: 4 where every
+// grain's 8 normals are 4 antipodal pairs (checked on the host), else 8.
+// The per-phase loops are kept rolled, and each kernel is compiled for one
+// NT: unrolled or duplicated copies of this body made the kernels wait on
+// instruction fetch.
+template <int S, int NA, bool HEAVY, int NT>
 __device__ __forceinline__ void update_cell(const In &in, const Out &out, const Mats &M, const Params &P, int l,
                                             int m, int k, uint32_t c, int n, const int (&ids)[NA],
                                             const float (&vc)[NA], const float (&lap)[NA], const float (&vL)[7],
@@ -487,20 +486,13 @@ __device__ __forceinline__ void update_cell(const In &in, const Out &out, const 
 #pragma unroll 1
             for (int t = 1; t < nn; ++t) {
                 const float *ug = M.n111 + (size_t)(P.n111_base + ids[t]) * 24;
-                float un[24];
-                if (P.sym_normals) {
+                float un[3 * NT];
 #pragma unroll
-                    for (int q = 0; q < 12; ++q) un[q] = __ldg(ug + q);
-                    interface_terms<4>(P, G, vL, h2, un, P.use_torque != 0, lap_sl[t], b_sl[t]);
-                } else {
-#pragma unroll
-                    for (int q = 0; q < 24; ++q) un[q] = __ldg(ug + q);
-                    interface_terms<8>(P, G, vL, h2, un, P.use_torque != 0, lap_sl[t], b_sl[t]);
-                }
+                for (int q = 0; q < 3 * NT; ++q) un[q] = __ldg(ug + q);
+                interface_terms<NT>(P, G, vL, h2, un, P.use_torque != 0, lap_sl[t], b_sl[t]);
             }
             if (ts > 0) {
-                const Facet fs = facet(gs, M.n111 + (size_t)(P.n111_base + ids[ts]) * 24, P.g2_floor,
-                                       P.sym_normals != 0);
+                const Facet fs = facet_n<NT>(gs, M.n111 + (size_t)(P.n111_base + ids[ts]) * 24, P.g2_floor);
                 const float al = calc_a(P, fs.cabs);
                 w_sl = P.w0 * (al * al);
             }
@@ -610,8 +602,9 @@ __device__ __forceinline__ void update_cell(const In &in, const Out &out, const 
 }
 
 // Update of one cell whose neighbourhood is not uniform: the 7-way merge of
-// the neighbour lists, then update_cell over up to AMAX active phases.
-template <int S, int AMAX, bool HEAVY>
+// the neighbour lists, then update_cell over up to AMAX active phases (NT:
+// normals per grain, used by the HEAVY form only).
+template <int S, int AMAX, bool HEAVY, int NT = 4>
 __device__ __forceinline__ void process_cell(const In &in, const Out &out, const Mats &M, const Params &P,
                                              int32_t *__restrict__ err, int l, int m, int k) {
     const uint32_t cells = P.cells32;
@@ -635,7 +628,7 @@ __device__ __forceinline__ void process_cell(const In &in, const Out &out, const
         }
         return;
     }
-    update_cell<S, AMAX, HEAVY>(in, out, M, P, l, m, k, c, A.n, A.ids, A.vc, A.lap, A.vL, A.ts, A.gs, err);
+    update_cell<S, AMAX, HEAVY, NT>(in, out, M, P, l, m, k, c, A.n, A.ids, A.vc, A.lap, A.vL, A.ts, A.gs, err);
 }
 
 // Kernel 1 of a step: every cell.  Uniform neighbourhoods (the cell and its
@@ -1069,8 +1062,9 @@ __global__ void __launch_bounds__(256) general_kernel(In in, Out out, Mats M, Pa
 }
 
 // Kernel 3 of a step: the queued solid-liquid interface cells, one thread
-// per cell, all lanes of a warp on the same (heavy) path.
-template <int S, int AMAX>
+// per cell, all lanes of a warp on the same (heavy) path; NT normals per
+// grain (4 or 8, from P.sym_normals).
+template <int S, int AMAX, int NT>
 __global__ void __launch_bounds__(128, 5) interface_kernel(In in, Out out, Mats M, Params P, Queue Q, int parity,
                                                            int32_t *__restrict__ err) {
     const uint32_t na = *(volatile uint32_t *)(Q.count + 2 * parity + 1);
@@ -1082,7 +1076,7 @@ __global__ void __launch_bounds__(128, 5) interface_kernel(In in, Out out, Mats 
         const uint32_t r = c - (uint32_t)k * plane;
         const int m = (int)(r / (uint32_t)P.nx);
         const int l = (int)(r - (uint32_t)m * (uint32_t)P.nx);
-        process_cell<S, AMAX, true>(in, out, M, P, err, l, m, k);
+        process_cell<S, AMAX, true, NT>(in, out, M, P, err, l, m, k);
     }
 }
 
@@ -1223,7 +1217,7 @@ __global__ void __launch_bounds__(256) batched_sweep_kernel(In in, Out out, Para
                    P.base + (uint32_t)m * (uint32_t)P.nx + (uint32_t)l, k0);
 }
 
-template <int S, int AMAX, bool HEAVY>
+template <int S, int AMAX, bool HEAVY, int NT = 4>
 __global__ void __launch_bounds__(HEAVY ? 128 : 256) batched_queue_kernel(In in, Out out, Mats M, Params P0,
                                                                           const mpf3d_instance *__restrict__ inst,
                                                                           int n_inst, Queue Q, int parity,
@@ -1240,7 +1234,7 @@ __global__ void __launch_bounds__(HEAVY ? 128 : 256) batched_queue_kernel(In in,
         const uint32_t r = r0 - (uint32_t)k * plane;
         const int m = (int)(r / (uint32_t)I.nx);
         const int l = (int)(r - (uint32_t)m * (uint32_t)I.nx);
-        process_cell<S, AMAX, HEAVY>(in, out, M, P, err, l, m, k);
+        process_cell<S, AMAX, HEAVY, NT>(in, out, M, P, err, l, m, k);
     }
 }
 
@@ -1502,7 +1496,10 @@ void launch_step(const In &in, const Out &out, const Mats &M, const Params &P, c
             general_kernel<S, AMAX><<<g_general, T.general_threads, 0, st>>>(in, out, M, P, Q, parity, err);
         },
         [&](cudaStream_t st) {
-            interface_kernel<S, AMAX><<<g_iface, T.iface_threads, 0, st>>>(in, out, M, P, Q, parity, err);
+            if (P.sym_normals)
+                interface_kernel<S, AMAX, 4><<<g_iface, T.iface_threads, 0, st>>>(in, out, M, P, Q, parity, err);
+            else
+                interface_kernel<S, AMAX, 8><<<g_iface, T.iface_threads, 0, st>>>(in, out, M, P, Q, parity, err);
         });
 }
 
@@ -1647,8 +1644,11 @@ void launch_batched(const In &in, const Out &out, const Mats &M, const Params &P
     const int sms = sms_of_current_device();
     batched_queue_kernel<S, AMAX, false><<<sms * T.general_blocks_per_sm, T.general_threads, 0, s>>>(
         in, out, M, P0, inst, n_inst, Q, parity, err);
-    if (P0.use_aniso)
-        batched_queue_kernel<S, AMAX, true><<<sms * T.iface_blocks_per_sm, T.iface_threads, 0, s>>>(
+    if (P0.use_aniso && P0.sym_normals)
+        batched_queue_kernel<S, AMAX, true, 4><<<sms * T.iface_blocks_per_sm, T.iface_threads, 0, s>>>(
+            in, out, M, P0, inst, n_inst, Q, parity, err);
+    else if (P0.use_aniso)
+        batched_queue_kernel<S, AMAX, true, 8><<<sms * T.iface_blocks_per_sm, T.iface_threads, 0, s>>>(
             in, out, M, P0, inst, n_inst, Q, parity, err);
 }
 
