@@ -55,6 +55,40 @@ def test_fp32_step_matches_fp64_oracle(aniso, torque):
     assert np.abs(got.sum(axis=0) - 1.0).max() < 1e-5
 
 
+def test_eight_normal_kernels_equal_four_normal_kernels():
+    """For the reference's antipodal {111} sets the interface kernels search 4
+    normals; the 8-normal build must give the same state bit for bit (|cos|
+    ties exactly within an antipodal pair, the first maximum is kept)."""
+    from mpf3d import inputs
+    case = inputs.voronoi_case(24, 16, 24, 6, 8, seed=4, orientation_seed=9)
+    a, b = make_solver(case), make_solver(case)
+    assert a.symmetric_normals
+    b.symmetric_normals = False
+    a.step(6)
+    b.step(6)
+    assert np.array_equal(a.to_dense(), b.to_dense())
+
+
+def test_fp32_step_with_general_normals_matches_fp64_oracle():
+    """Normals that are not antipodal pairs (rows 4..7 turned off their
+    pairs) run the 8-normal kernels; they still match the FP64 oracle."""
+    from mpf3d import inputs
+    base = inputs.voronoi_case(24, 16, 24, 6, 8, seed=4, orientation_seed=9)
+    rng = np.random.default_rng(3)
+    n111 = base.n111.astype(np.float64).copy()
+    n111[:, 4:8] += rng.normal(scale=0.2, size=n111[:, 4:8].shape)
+    n111 /= np.linalg.norm(n111, axis=2, keepdims=True)
+    case = inputs.Case(base.phi, base.temp, base.quats, n111.astype(np.float32), base.wij, base.aij, base.mij,
+                       base.phys)
+    steps = 5
+    ref, _ = oracle_fp64(case, steps)
+    s = make_solver(case)
+    assert not s.symmetric_normals
+    s.step(steps)
+    err = np.abs(s.to_dense(np.float64) - ref).max()
+    assert err <= TOL, f"max|dphi| = {err:.3e}"
+
+
 def test_fp32_undercooled_junctions():
     from mpf3d import inputs
     case = inputs.voronoi_case(20, 20, 20, 10, 8, seed=7, orientation_seed=3, undercooling=3.0)
