@@ -161,7 +161,8 @@ int mpf3d_compact_active_count(const uint32_t *head, const uint16_t *idx, int sl
  * a2ij = aij*aij elementwise (float32).  T0z: float64 [nz].
  * symmetric_normals != 0 asserts that every grain's n111 rows 4..7 are the
  * exact negatives of rows 3..0 (true for the rotated (+-1,+-1,+-1)/sqrt(3)
- * set of src/orientation_utils.py:182-212), which halves the facet search.
+ * set of src/orientation_utils.py:182-212), which halves the facet search
+ * (the interface kernel is built once for 4 and once for 8 normals).
  * Scratch: work_items uint32[cells] (cells handed from the sweep kernel to
  * the general and interface kernels of the step) and work_count uint32[4],
  * zeroed once before the first step; `parity` alternates 0/1 on consecutive
