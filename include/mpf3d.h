@@ -351,14 +351,25 @@ int mpf3d_batched_step(const uint32_t *head, const uint16_t *idx, const float *v
  * kernels from `tuning` (its general_* and iface_* fields; the sweep's 32 x 8 x
  * 4 tiles are fixed by the instance table, so sweep_zb and sweep_by must be
  * valid but are not used).  NULL: {8 x 256, 8 x 128} blocks per SM.  Every
- * shape computes the same result. */
+ * shape computes the same result.
+ *
+ * tile_flags (uint8, mpf3d_batched_tile_flags_len(n_tiles) bytes, or NULL):
+ * quiet-tile flags of the batched sweep, as for mpf3d_compact_step_tuned,
+ * per 32 x 1 x 4 warp tile of each instance.  Zero them before the first
+ * step and whenever the state buffers are written other than by this
+ * function (initialisation, restore); steps must alternate parity.  Same
+ * results with and without them. */
 int mpf3d_batched_step_tuned(const uint32_t *head, const uint16_t *idx, const float *val, uint32_t *head_out,
                              uint16_t *idx_out, float *val_out, int slots, int amax, const mpf3d_instance *inst,
                              int n_inst, int n_tiles, uint32_t total_cells, const float *wij, const float *a2ij,
                              const float *mij, const float *n111, int N, const mpf3d_scalars *scalars,
                              int enable_anisotropy, int enable_torque, int symmetric_normals, uint32_t *work_items,
                              uint32_t *work_count, int parity, int32_t *err, void *stream, int options,
-                             const mpf3d_tuning *tuning);
+                             const mpf3d_tuning *tuning, uint8_t *tile_flags);
+
+/* bytes of the batched step's quiet-tile flags: 2 parities x 8 warp tiles
+ * per sweep tile (0 for n_tiles <= 0) */
+int64_t mpf3d_batched_tile_flags_len(int n_tiles);
 
 /* Observables per instance, accumulated into zeroed float64 arrays:
  * acc[6*i..6*i+5] = {sum of front heights left of split, columns left, sum

@@ -1183,10 +1183,17 @@ __device__ __forceinline__ Params instance_params(const Params &P0, const mpf3d_
     return P;
 }
 
+// The batched sweep.  One block is one 32 x 8 x SWEEP_ZB tile of one
+// instance, and each of its 8 warps one 32 x 1 x SWEEP_ZB warp tile, whose
+// index is blockIdx.x * 8 + threadIdx.y.  With `flags` (2 x 8 x n_tiles
+// bytes, halves alternating with the step parity; NULL: every tile visited)
+// a warp tile that was uniform in the previous step together with its 6 face
+// neighbours in the same instance (periodic x and y, clamped z) is quiet and
+// skipped, by the argument of the single-domain sweep's quiet tiles.
 template <int S, int AMAX>
 __global__ void __launch_bounds__(256) batched_sweep_kernel(In in, Out out, Params P0,
                                                             const mpf3d_instance *__restrict__ inst, int n_inst,
-                                                            Queue Q, int parity) {
+                                                            Queue Q, int parity, uint8_t *__restrict__ flags) {
     __shared__ uint32_t s_cnt[3], s_base[3];
     const int tlin = threadIdx.x + 32 * threadIdx.y;
     if (tlin < 3) s_cnt[tlin] = 0;
@@ -1197,14 +1204,47 @@ __global__ void __launch_bounds__(256) batched_sweep_kernel(In in, Out out, Para
     const int i = find_instance_by_tile(inst, n_inst, (int)blockIdx.x);
     const mpf3d_instance I = inst[i];
     const int t = (int)blockIdx.x - I.tile_start;
-    const int tx = (I.nx + 31) / 32, ty = (I.ny + 7) / 8;
-    const int l = (t % tx) * 32 + threadIdx.x;
+    const int tx = (I.nx + 31) / 32, ty = (I.ny + 7) / 8, tz = (I.nz + SWEEP_ZB - 1) / SWEEP_ZB;
+    const int bx = t % tx, kb = t / (tx * ty);
+    const int l = bx * 32 + threadIdx.x;
     const int m = ((t / tx) % ty) * 8 + threadIdx.y;
-    const int k0 = (t / (tx * ty)) * SWEEP_ZB;
-    const bool inside = l < I.nx && m < I.ny && k0 < I.nz;
+    const int k0 = kb * SWEEP_ZB;
+    const bool row_in = m < I.ny && k0 < I.nz;  // the same for the 32 lanes of a warp
+    const bool inside = l < I.nx && row_in;
     const Params P = instance_params(P0, I);
     BlockSink<SWEEP_ZB> sink(s_cnt);
-    if (inside) sweep_column(in, out, P, Q.split, sink, l, m, k0);
+    if (!flags) {
+        if (inside) sweep_column(in, out, P, Q.split, sink, l, m, k0);
+    } else {
+        const uint32_t nw = gridDim.x * 8u;
+        const uint8_t *fin = flags + (size_t)(parity ^ 1) * nw;
+        uint8_t *fout = flags + (size_t)parity * nw;
+        const uint32_t w = blockIdx.x * 8u + threadIdx.y;
+        const bool lane0 = threadIdx.x == 0;
+        if (!row_in) {
+            if (lane0) fout[w] = 1;
+        } else {
+            // warp tile (x tile a, row mm, z tile c) of this instance
+            auto wt = [&](int a, int mm, int c) {
+                return (uint32_t)(I.tile_start + (c * ty + mm / 8) * tx + a) * 8u + (uint32_t)(mm % 8);
+            };
+            // the 7 flags are loaded together (no short-circuit chain of loads)
+            const uint32_t f0 = fin[w];
+            const uint32_t f1 = fin[wt(bx + 1 < tx ? bx + 1 : 0, m, kb)];
+            const uint32_t f2 = fin[wt(bx > 0 ? bx - 1 : tx - 1, m, kb)];
+            const uint32_t f3 = fin[wt(bx, m + 1 < I.ny ? m + 1 : 0, kb)];
+            const uint32_t f4 = fin[wt(bx, m > 0 ? m - 1 : I.ny - 1, kb)];
+            const uint32_t f5 = fin[wt(bx, m, kb + 1 < tz ? kb + 1 : kb)];
+            const uint32_t f6 = fin[wt(bx, m, kb > 0 ? kb - 1 : kb)];
+            if ((f0 & f1 & f2 & f3 & f4 & f5 & f6) != 0u) {
+                if (lane0) fout[w] = 1;
+            } else {
+                const bool uni = l < I.nx ? sweep_column(in, out, P, Q.split, sink, l, m, k0) : true;
+                const bool all = __all_sync(0xffffffffu, uni);
+                if (lane0) fout[w] = all ? 1 : 0;
+            }
+        }
+    }
     __syncthreads();
     if (tlin < 3) {
         const uint32_t n = s_cnt[tlin];
@@ -1636,8 +1676,9 @@ Params shared_params(const mpf3d_scalars *sc, int enable_anisotropy, int enable_
 template <int S, int AMAX>
 void launch_batched(const In &in, const Out &out, const Mats &M, const Params &P0, const mpf3d_instance *inst,
                     int n_inst, int n_tiles, const Queue &Q, int parity, int32_t *err, cudaStream_t s,
-                    const mpf3d_tuning &T) {
-    batched_sweep_kernel<S, AMAX><<<n_tiles, dim3(32, 8, 1), 0, s>>>(in, out, P0, inst, n_inst, Q, parity);
+                    const mpf3d_tuning &T, uint8_t *tile_flags) {
+    batched_sweep_kernel<S, AMAX><<<n_tiles, dim3(32, 8, 1), 0, s>>>(in, out, P0, inst, n_inst, Q, parity,
+                                                                      tile_flags);
     // one stream: the side-by-side launch of the compact step measured no
     // gain here; the work-list grids come from T (the sweep's 32 x 8 x 4
     // tiles are fixed by the instance table)
@@ -1760,7 +1801,8 @@ extern "C" int mpf3d_batched_step_tuned(const uint32_t *head, const uint16_t *id
                                         const float *wij, const float *a2ij, const float *mij, const float *n111, int N,
                                         const mpf3d_scalars *sc, int enable_anisotropy, int enable_torque,
                                         int symmetric_normals, uint32_t *work_items, uint32_t *work_count, int parity,
-                                        int32_t *err, void *stream, int options, const mpf3d_tuning *tuning) {
+                                        int32_t *err, void *stream, int options, const mpf3d_tuning *tuning,
+                                        uint8_t *tile_flags) {
     const mpf3d_tuning T = tuning ? *tuning : kBatchedDefault;
     if (!tuning_ok(T)) return MPF3D_ERR_ARG;
     if (!head || !idx || !val || !head_out || !idx_out || !val_out || !inst || !wij || !a2ij || !mij || !n111 ||
@@ -1779,11 +1821,16 @@ extern "C" int mpf3d_batched_step_tuned(const uint32_t *head, const uint16_t *id
     Queue Q{work_items, work_count, (options & MPF3D_STEP_MULTI_LIST) ? 1 : 0};
     cudaStream_t s = (cudaStream_t)stream;
     parity &= 1;
-    if (slots == 4 && amax == 8) launch_batched<4, 8>(in, out, M, P0, inst, n_inst, n_tiles, Q, parity, err, s, T);
-    else if (slots == 8 && amax == 16) launch_batched<8, 16>(in, out, M, P0, inst, n_inst, n_tiles, Q, parity, err, s, T);
-    else if (slots == 16 && amax == 32) launch_batched<16, 32>(in, out, M, P0, inst, n_inst, n_tiles, Q, parity, err, s, T);
+    uint8_t *F = tile_flags;
+    if (slots == 4 && amax == 8) launch_batched<4, 8>(in, out, M, P0, inst, n_inst, n_tiles, Q, parity, err, s, T, F);
+    else if (slots == 8 && amax == 16) launch_batched<8, 16>(in, out, M, P0, inst, n_inst, n_tiles, Q, parity, err, s, T, F);
+    else if (slots == 16 && amax == 32) launch_batched<16, 32>(in, out, M, P0, inst, n_inst, n_tiles, Q, parity, err, s, T, F);
     else return MPF3D_ERR_ARG;
     return cudaGetLastError() == cudaSuccess ? MPF3D_OK : MPF3D_ERR_CUDA;
+}
+
+extern "C" int64_t mpf3d_batched_tile_flags_len(int n_tiles) {
+    return n_tiles > 0 ? 16 * (int64_t)n_tiles : 0;
 }
 
 extern "C" int mpf3d_batched_step(const uint32_t *head, const uint16_t *idx, const float *val, uint32_t *head_out,
@@ -1796,7 +1843,7 @@ extern "C" int mpf3d_batched_step(const uint32_t *head, const uint16_t *idx, con
     return mpf3d_batched_step_tuned(head, idx, val, head_out, idx_out, val_out, slots, amax, inst, n_inst, n_tiles,
                                     total_cells, wij, a2ij, mij, n111, N, sc, enable_anisotropy, enable_torque,
                                     symmetric_normals, work_items, work_count, parity, err, stream, options,
-                                    nullptr);
+                                    nullptr, nullptr);
 }
 
 extern "C" int mpf3d_batched_fronts(const uint32_t *head, const uint16_t *idx, const float *val, int slots,

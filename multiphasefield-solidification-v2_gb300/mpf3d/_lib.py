@@ -89,7 +89,8 @@ _SIGS = {
                                   _VP, _I32, _VP, _VP, _I32]),
     "mpf3d_batched_step_tuned": (_I32, [_VP, _VP, _VP, _VP, _VP, _VP, _I32, _I32, _VP, _I32, _I32, ctypes.c_uint32,
                                         _VP, _VP, _VP, _VP, _I32, ctypes.POINTER(Scalars), _I32, _I32, _I32, _VP,
-                                        _VP, _I32, _VP, _VP, _I32, _VP]),
+                                        _VP, _I32, _VP, _VP, _I32, _VP, _VP]),
+    "mpf3d_batched_tile_flags_len": (_I64, [_I32]),
     "mpf3d_batched_fronts": (_I32, [_VP, _VP, _VP, _I32, _VP, _I32, ctypes.c_uint32, _VP, _VP]),
     "mpf3d_batched_gb_rows": (_I32, [_VP, _VP, _VP, _I32, _VP, _I32, ctypes.c_uint32, _VP, _VP, _VP]),
     "mpf3d_compact_init_owner": (_I32, [_VP, _I32, _VP, _I32, _I32, _I32, _I32, _VP, _VP, _VP, _VP]),

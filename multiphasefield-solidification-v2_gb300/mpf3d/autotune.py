@@ -173,7 +173,7 @@ def tune_batched(batch, steps: int = 8, use_cache: bool = True) -> dict:
             batch.cur, batch.step_count = cur, count
             for dst, src in zip(batch.buf[cur], snap):
                 dst.copy_(src)
-            batch.work_count.zero_()
+            batch.forget_history()
 
     trials = {}
     base = trial(DEFAULT)

@@ -121,6 +121,10 @@ class BatchedBicrystals:
         # the three work lists of MPF3D_STEP_MULTI_LIST and their counters
         self.work_items = torch.empty(2 * self.total_cells, dtype=torch.int32, device=self.device)
         self.work_count = torch.zeros(6, dtype=torch.int32, device=self.device)
+        # quiet-tile flags of the batched sweep (zero: the next step visits every tile)
+        n_flags = int(_lib.lib().mpf3d_batched_tile_flags_len(self.n_tiles))
+        self.tile_flags = torch.zeros(max(n_flags, 1), dtype=torch.uint8, device=self.device)
+        self.skip_quiet_tiles = True
         self.buf = [self._alloc(), self._alloc()]
         self.cur = 0
         self.step_count = 0
@@ -184,9 +188,18 @@ class BatchedBicrystals:
             ctypes.byref(self.scalars), int(self.anisotropy), int(self.torque), int(self.symmetric_normals),
             self.work_items.data_ptr(), self.work_count.data_ptr(), self.step_count & 1,
             self.err.data_ptr(), self._stream(), _lib.STEP_MULTI_LIST,
-            ctypes.byref(self.tuning) if self.tuning is not None else None)
+            ctypes.byref(self.tuning) if self.tuning is not None else None,
+            self.tile_flags.data_ptr() if self.skip_quiet_tiles else None)
         _lib.check(rc, "batched_step")
         self.cur = 1 - self.cur
+
+    def forget_history(self) -> None:
+        """Clear what the step keeps from earlier steps -- the quiet-tile flags
+        and the work-list counters.  Required after the state buffers are
+        written other than by a step (restore); the next step then visits
+        every tile."""
+        self.tile_flags.zero_()
+        self.work_count.zero_()
 
     def autotune(self, steps: int = 8, use_cache: bool = True) -> dict:
         """Pick the fastest work-list kernel shape for this batch (see
