@@ -1045,9 +1045,10 @@ __global__ void __launch_bounds__(512, 3) sweep_kernel_tma(const __grid_constant
 }
 
 // Kernel 2 of a step: the cells queued for the general update, one thread
-// per cell.
+// per cell.  Capped at 48 registers (5 blocks of 256 per SM): it waits on
+// memory, and more resident warps beat the few spilled values.
 template <int S, int AMAX>
-__global__ void __launch_bounds__(256) general_kernel(In in, Out out, Mats M, Params P, Queue Q, int parity,
+__global__ void __launch_bounds__(256, 5) general_kernel(In in, Out out, Mats M, Params P, Queue Q, int parity,
                                                      int32_t *__restrict__ err) {
     const uint32_t n = *(volatile uint32_t *)(Q.count + 2 * parity);
     const uint32_t plane = (uint32_t)P.nx * (uint32_t)P.ny;
