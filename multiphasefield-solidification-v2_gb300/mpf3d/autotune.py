@@ -26,8 +26,8 @@ QUEUE = [(g, gt, i, it) for (g, gt), (i, it) in itertools.product([(4, 256), (8,
 
 
 def cache_path() -> str:
-    return os.environ.get("MPF3D_TUNING_CACHE",
-                          os.path.join(os.path.expanduser("~"), ".cache", "mpf3d", "tuning.json"))
+    return os.path.abspath(os.environ.get("MPF3D_TUNING_CACHE",
+                                          os.path.join(os.path.expanduser("~"), ".cache", "mpf3d", "tuning.json")))
 
 
 def make(cfg) -> _lib.Tuning:
