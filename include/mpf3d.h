@@ -242,6 +242,33 @@ int mpf3d_compact_step_tuned(const uint32_t *head, const uint16_t *idx, const fl
 /* Bytes of tile_flags for an nx x ny x nz domain (any sweep_zb). */
 int64_t mpf3d_compact_tile_flags_len(int nx, int ny, int nz);
 
+/* Device step clock of mpf3d_compact_step_clocked (device memory, 8-byte
+ * aligned).  step[parity] holds the index of the step about to run with that
+ * parity; the caller sets it once (step[n & 1] = n before step n) and each
+ * step advances it.  tmc[] is written by the step for its own kernels. */
+typedef struct mpf3d_step_clock {
+    int64_t step[2];
+    double tmc[2];
+} mpf3d_step_clock;
+
+/* mpf3d_compact_step_tuned with the step's temperature taken from the device:
+ * the step reads its index s = clock->step[parity], runs at
+ * Tm_plus_cool = T_melt + s * cooling_rate (float64, rounded operation by
+ * operation: the same value as the host computing that expression) and
+ * sets clock->step[parity ^ 1] = s + 1.  Nothing of the step is then passed
+ * by value but its parity, so a CUDA graph of an even number of captured
+ * steps can be replayed over and over and keeps cooling (the reference's
+ * kernel_update_temp_3d, src/gpu_kernels_3d.py:833-838, applied once per
+ * step).  Same results as mpf3d_compact_step_tuned at the same step index. */
+int mpf3d_compact_step_clocked(const uint32_t *head, const uint16_t *idx, const float *val, uint32_t *head_out,
+                               uint16_t *idx_out, float *val_out, int slots, int amax, const double *T0z,
+                               mpf3d_step_clock *clock, double T_melt, double cooling_rate, const float *wij,
+                               const float *a2ij, const float *mij, const float *n111, int N, int nx, int ny,
+                               int nz, const mpf3d_scalars *scalars, int enable_anisotropy, int enable_torque,
+                               int symmetric_normals, uint32_t *work_items, uint32_t *work_count, int parity,
+                               int32_t *err, void *stream, const mpf3d_tuning *tuning, uint8_t *tile_flags,
+                               int options);
+
 /* compact state -> dense phi of one domain stored at cells [base, base +
  * nx*ny*nz) of state arrays whose slot planes are `stride` cells apart. */
 int mpf3d_compact_to_dense_view(const uint32_t *head, const uint16_t *idx, const float *val, int slots,

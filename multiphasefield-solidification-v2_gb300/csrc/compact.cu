@@ -51,6 +51,15 @@ struct Params {
     float inv_dx2, inv_2dx, half_over_dx, inv_dx, dt;
     float eps0, eps0sq, w0, mu_a, delta_a, mu_da, pp, tan_a0, g2_floor, ksi, theta_c, cos_theta_lo, Sf;
     double Tmc;  // T_melt + accumulated cooling (float64)
+    // Device step clock (null: Tmc above).  The sweep reads the step's index
+    // s = clock->step[parity], writes clock->tmc[parity] = clock_T_melt +
+    // s * clock_rate (rounded operation by operation, like the host's
+    // float64 expression) for the work-list kernels and clock->step[parity ^
+    // 1] = s + 1 for the next step, so a CUDA graph of steps keeps cooling
+    // when it is replayed.
+    mpf3d_step_clock *clock;
+    double clock_T_melt, clock_rate;
+    int parity;
     int use_aniso, use_torque;
     int sym_normals;  // every grain's n111 rows 4..7 are -(rows 3..0)
     // per-domain view (a batch of instances shares the state arrays)
@@ -531,7 +540,8 @@ __device__ __forceinline__ void update_cell(const In &in, const Out &out, const 
         W[t1] = w;
         Ag[t1] = a;
     }
-    const float dT = P.t_uniform ? P.dT_uniform : (float)(M.T0z[k] - P.Tmc);
+    const double Tmc = P.clock ? P.clock->tmc[P.parity] : P.Tmc;
+    const float dT = P.t_uniform ? P.dT_uniform : (float)(M.T0z[k] - Tmc);
     const float inv_n = 1.0f / (float)(n > 0 ? n : 1);
     float outv[NA];
 #pragma unroll 1
@@ -825,6 +835,15 @@ __host__ __device__ __forceinline__ uint32_t tiles_of(int nx, int ny, int nz) {
     return (uint32_t)((nz + ZB - 1) / ZB) * (uint32_t)ny * (uint32_t)((nx + 31) / 32);
 }
 
+// One thread of the sweep advances the device step clock (Params::clock):
+// the step's T_melt + cooling for the work-list kernels, the next index.
+__device__ __forceinline__ void advance_clock(const Params &P) {
+    if (!P.clock) return;
+    const int64_t s = P.clock->step[P.parity];
+    P.clock->tmc[P.parity] = __dadd_rn(P.clock_T_melt, __dmul_rn((double)s, P.clock_rate));
+    P.clock->step[P.parity ^ 1] = s + 1;
+}
+
 // 40 registers (3 blocks of 512 per SM): more resident warps beat keeping
 // ZB = 8 columns in registers; the tuner then prefers ZB = 4
 template <int S, int AMAX, int ZB = SWEEP_ZB>
@@ -836,6 +855,7 @@ __global__ void __launch_bounds__(512, 3) sweep_kernel(In in, Out out, Mats M, P
     const int k0 = (blockIdx.z * blockDim.z + threadIdx.z) * ZB;
     const int tlin = threadIdx.x + (int)blockDim.x * threadIdx.y;  // blockDim.z is 1
     if (tlin < 3) s_cnt[tlin] = 0;
+    if (blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && tlin == 3 && threadIdx.z == 0) advance_clock(P);
     if (blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.x < 2 && threadIdx.y == 0 &&
         threadIdx.z == 0)
         Q.count[2 * (parity ^ 1) + threadIdx.x] = 0;  // the previous step's kernels are done with them
@@ -941,6 +961,8 @@ __global__ void __launch_bounds__(512, 3) sweep_kernel_tma(const __grid_constant
         Q.count[2 * (parity ^ 1) + threadIdx.x] = 0;  // the previous step's kernels are done with them
     if (blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.y == 0 && threadIdx.x == 2 && Q.split)
         Q.count[4 + (parity ^ 1)] = 0;
+    if (blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.y == 0 && threadIdx.x == 3)
+        advance_clock(P);
     // quiet flags of this warp's tile (as sweep_kernel)
     const bool row_ok = m < P.ny && k0 < P.nz;
     bool quiet = false;
@@ -1707,14 +1729,16 @@ extern "C" int mpf3d_streams_prepare(void *stream) {
     return side_ready(side, (cudaStream_t)stream) ? MPF3D_OK : MPF3D_ERR_CUDA;
 }
 
-extern "C" int mpf3d_compact_step_tuned(const uint32_t *cnt, const uint16_t *idx, const float *val,
-                                        uint32_t *cnt_out, uint16_t *idx_out, float *val_out, int slots, int amax,
-                                        const double *T0z, double Tm_plus_cool, const float *wij, const float *a2ij,
-                                        const float *mij, const float *n111, int N, int nx, int ny, int nz,
-                                        const mpf3d_scalars *sc, int enable_anisotropy, int enable_torque,
-                                        int symmetric_normals, uint32_t *work_items, uint32_t *work_count,
-                                        int parity, int32_t *err, void *stream, const mpf3d_tuning *tuning,
-                                        uint8_t *tile_flags, int options) {
+// The body of mpf3d_compact_step_tuned and mpf3d_compact_step_clocked
+// (clock: null, or the device step clock with T_melt and the cooling rate).
+static int compact_step_impl(const uint32_t *cnt, const uint16_t *idx, const float *val, uint32_t *cnt_out,
+                             uint16_t *idx_out, float *val_out, int slots, int amax, const double *T0z,
+                             double Tm_plus_cool, const float *wij, const float *a2ij, const float *mij,
+                             const float *n111, int N, int nx, int ny, int nz, const mpf3d_scalars *sc,
+                             int enable_anisotropy, int enable_torque, int symmetric_normals, uint32_t *work_items,
+                             uint32_t *work_count, int parity, int32_t *err, void *stream,
+                             const mpf3d_tuning *tuning, uint8_t *tile_flags, int options, mpf3d_step_clock *clock,
+                             double clock_T_melt, double clock_rate) {
     const mpf3d_tuning T = tuning ? *tuning : kDefaultTuning;
     if (!tuning_ok(T)) return MPF3D_ERR_ARG;
     if (!cnt || !idx || !val || !cnt_out || !idx_out || !val_out || !T0z || !wij || !a2ij || !mij || !n111 || !sc ||
@@ -1728,11 +1752,15 @@ extern "C" int mpf3d_compact_step_tuned(const uint32_t *cnt, const uint16_t *idx
     P.cells = (int64_t)nx * ny * nz;
     P.cells32 = (uint32_t)P.cells;
     P.Tmc = Tm_plus_cool;
+    parity &= 1;
+    P.clock = clock;
+    P.clock_T_melt = clock_T_melt;
+    P.clock_rate = clock_rate;
+    P.parity = parity;
     In in{cnt, idx, val};
     Out out{cnt_out, idx_out, val_out};
     Mats M{T0z, wij, a2ij, mij, n111};
     Queue Q{work_items, work_count, (options & MPF3D_STEP_MULTI_LIST) ? 1 : 0};
-    parity &= 1;
     cudaStream_t s = (cudaStream_t)stream;
     const bool tma = (options & MPF3D_STEP_SWEEP_TMA) != 0;
     if (slots == 4 && amax == 8) launch_step<4, 8>(in, out, M, P, Q, parity, tile_flags, err, s, T, tma);
@@ -1740,6 +1768,36 @@ extern "C" int mpf3d_compact_step_tuned(const uint32_t *cnt, const uint16_t *idx
     else if (slots == 16 && amax == 32) launch_step<16, 32>(in, out, M, P, Q, parity, tile_flags, err, s, T, tma);
     else return MPF3D_ERR_ARG;
     return cudaGetLastError() == cudaSuccess ? MPF3D_OK : MPF3D_ERR_CUDA;
+}
+
+extern "C" int mpf3d_compact_step_tuned(const uint32_t *cnt, const uint16_t *idx, const float *val,
+                                        uint32_t *cnt_out, uint16_t *idx_out, float *val_out, int slots, int amax,
+                                        const double *T0z, double Tm_plus_cool, const float *wij, const float *a2ij,
+                                        const float *mij, const float *n111, int N, int nx, int ny, int nz,
+                                        const mpf3d_scalars *sc, int enable_anisotropy, int enable_torque,
+                                        int symmetric_normals, uint32_t *work_items, uint32_t *work_count,
+                                        int parity, int32_t *err, void *stream, const mpf3d_tuning *tuning,
+                                        uint8_t *tile_flags, int options) {
+    return compact_step_impl(cnt, idx, val, cnt_out, idx_out, val_out, slots, amax, T0z, Tm_plus_cool, wij, a2ij,
+                             mij, n111, N, nx, ny, nz, sc, enable_anisotropy, enable_torque, symmetric_normals,
+                             work_items, work_count, parity, err, stream, tuning, tile_flags, options, nullptr, 0.0,
+                             0.0);
+}
+
+extern "C" int mpf3d_compact_step_clocked(const uint32_t *cnt, const uint16_t *idx, const float *val,
+                                          uint32_t *cnt_out, uint16_t *idx_out, float *val_out, int slots,
+                                          int amax, const double *T0z, mpf3d_step_clock *clock, double T_melt,
+                                          double cooling_rate, const float *wij, const float *a2ij,
+                                          const float *mij, const float *n111, int N, int nx, int ny, int nz,
+                                          const mpf3d_scalars *sc, int enable_anisotropy, int enable_torque,
+                                          int symmetric_normals, uint32_t *work_items, uint32_t *work_count,
+                                          int parity, int32_t *err, void *stream, const mpf3d_tuning *tuning,
+                                          uint8_t *tile_flags, int options) {
+    if (!clock) return MPF3D_ERR_ARG;
+    return compact_step_impl(cnt, idx, val, cnt_out, idx_out, val_out, slots, amax, T0z, T_melt, wij, a2ij, mij,
+                             n111, N, nx, ny, nz, sc, enable_anisotropy, enable_torque, symmetric_normals,
+                             work_items, work_count, parity, err, stream, tuning, tile_flags, options, clock, T_melt,
+                             cooling_rate);
 }
 
 extern "C" int mpf3d_compact_step(const uint32_t *cnt, const uint16_t *idx, const float *val, uint32_t *cnt_out,

@@ -113,6 +113,9 @@ _SIGS = {
     "mpf3d_compact_step_tuned": (_I32, [_VP, _VP, _VP, _VP, _VP, _VP, _I32, _I32, _VP, _F64, _VP, _VP, _VP, _VP,
                                         _I32, _I32, _I32, _I32, ctypes.POINTER(Scalars), _I32, _I32, _I32,
                                         _VP, _VP, _I32, _VP, _VP, ctypes.POINTER(Tuning), _VP, _I32]),
+    "mpf3d_compact_step_clocked": (_I32, [_VP, _VP, _VP, _VP, _VP, _VP, _I32, _I32, _VP, _VP, _F64, _F64, _VP, _VP,
+                                          _VP, _VP, _I32, _I32, _I32, _I32, ctypes.POINTER(Scalars), _I32, _I32,
+                                          _I32, _VP, _VP, _I32, _VP, _VP, ctypes.POINTER(Tuning), _VP, _I32]),
     "mpf3d_compact_tile_flags_len": (_I64, [_I32, _I32, _I32]),
     "mpf3d_compact_step_noalloc": (_I32, [_VP, _VP, _VP, _VP, _VP, _VP, _I32, _I32, _VP, _F64, _VP, _VP,
                                           _VP, _VP, _I32, _I32, _I32, _I32, ctypes.POINTER(Scalars),

@@ -150,6 +150,11 @@ class CompactSolver:
         n_flags = int(_lib.lib().mpf3d_compact_tile_flags_len(self.nx, self.ny, self.nz))
         self.tile_flags = torch.zeros(max(n_flags, 1), dtype=torch.uint8, device=self.device)
         self._tiles_zb = None
+        # device step clock (mpf3d_step_clock: int64 step[2], float64 tmc[2])
+        # and the step index it holds for the next step (None: unknown)
+        self.clock = torch.zeros(4, dtype=torch.int64, device=self.device)
+        self._clock_next = None
+        self.graph = None  # CUDA graph of captured steps (capture())
 
     def forget_history(self) -> None:
         """Clear what the step keeps from earlier steps -- the quiet-tile flags
@@ -197,21 +202,24 @@ class CompactSolver:
     def launch_step(self, step_index: int) -> None:
         """Enqueue one step (no synchronisation); step_index is 1-based.
 
-        The step's temperature (T_melt + step_index * cooling_rate) and its
-        parity are passed by value.  A CUDA graph captured around this call
-        therefore replays the recorded steps as they were: with cooling it
-        is valid for one replay; an isothermal run may replay a graph of an
-        even number of steps repeatedly."""
+        The step runs at T_melt + step_index * cooling_rate, which it reads
+        from the solver's device clock (mpf3d_compact_step_clocked); the clock
+        is set here only when step_index is not the step that follows the
+        last one launched.  Only the parity is passed by value, so a CUDA
+        graph of an even number of consecutive steps (capture()) can be
+        replayed over and over and keeps cooling."""
         src = self.buf[self.cur]
         dst = self.buf[1 - self.cur]
-        tmc = self.T_melt + step_index * self.cooling_rate
         zb = self.tuning.sweep_zb if self.tuning is not None else 4
         if zb != self._tiles_zb:  # the tile geometry follows the sweep shape
             self.tile_flags.zero_()
             self._tiles_zb = zb
-        rc = _lib.lib().mpf3d_compact_step_tuned(
+        if step_index != self._clock_next:
+            self.clock[step_index & 1].fill_(step_index)  # a kernel: no host copy, capturable
+        rc = _lib.lib().mpf3d_compact_step_clocked(
             src[0].data_ptr(), src[1].data_ptr(), src[2].data_ptr(), dst[0].data_ptr(),
-            dst[1].data_ptr(), dst[2].data_ptr(), self.slots, self.amax, self.T0z.data_ptr(), tmc,
+            dst[1].data_ptr(), dst[2].data_ptr(), self.slots, self.amax, self.T0z.data_ptr(),
+            self.clock.data_ptr(), self.T_melt, self.cooling_rate,
             self.wij.data_ptr(), self.a2ij.data_ptr(), self.mij.data_ptr(), self.n111.data_ptr(),
             self.N, self.nx, self.ny, self.nz, ctypes.byref(self.scalars), int(self.anisotropy),
             int(self.torque), int(self.symmetric_normals), self.work_items.data_ptr(),
@@ -220,26 +228,73 @@ class CompactSolver:
             self.tile_flags.data_ptr() if self.skip_quiet_tiles else None,
             _lib.STEP_MULTI_LIST | (_lib.STEP_SWEEP_TMA if self.sweep_tma else 0))
         _lib.check(rc, "compact_step")
+        self._clock_next = step_index + 1
         self.cur = 1 - self.cur
 
-    def step(self, n: int = 1, check: bool = True, check_every: int = 200) -> None:
-        """Advance n steps.  With check=True the device error word is read
-        every `check_every` steps; a slot overflow rolls the state back to the
-        start of that chunk, widens the slot template (4 -> 8 -> 16) and
-        redoes the chunk, so no phase is ever dropped silently."""
-        n = int(n)
-        if not check:
-            for _ in range(n):
+    def capture(self, steps: int) -> None:
+        """Capture `steps` (even) consecutive steps, starting at the next one,
+        in a CUDA graph; step() then replays it wherever it fits (same
+        buffers and parity) and launches the rest one by one.  Capture after
+        autotune() and after setting sweep_tma / skip_quiet_tiles: the graph
+        keeps the launch shape it was captured with."""
+        torch = _torch()
+        steps = int(steps)
+        if steps <= 0 or steps % 2:
+            raise ValueError("capture an even number of steps so the buffers and parities line up")
+        n0 = self.step_count + 1
+        zb = self.tuning.sweep_zb if self.tuning is not None else 4
+        if zb != self._tiles_zb:
+            self.tile_flags.zero_()
+            self._tiles_zb = zb
+        if self._clock_next != n0:  # set outside the graph: a replay must not reset it
+            self.clock[n0 & 1].fill_(n0)
+            self._clock_next = n0
+        cs = torch.cuda.Stream(self.device)
+        cs.wait_stream(torch.cuda.current_stream(self.device))
+        _lib.check(_lib.lib().mpf3d_streams_prepare(cs.cuda_stream), "streams_prepare")
+        g = torch.cuda.CUDAGraph()
+        cur0 = self.cur
+        with torch.cuda.graph(g, stream=cs):
+            for i in range(steps):
+                self.launch_step(n0 + i)
+        torch.cuda.current_stream(self.device).wait_stream(cs)
+        # the capture recorded the steps without running them
+        self.cur, self._clock_next = cur0, n0
+        self.graph, self.graph_steps, self._graph_at = g, steps, (cur0, n0 & 1, self.buf[cur0][0].data_ptr())
+
+    def _advance(self, n: int) -> None:
+        """Launch n steps: graph replays where the captured graph fits, the
+        rest one by one."""
+        while n > 0:
+            g = self.graph
+            if (g is not None and n >= self.graph_steps and
+                    self._graph_at == (self.cur, (self.step_count + 1) & 1, self.buf[self.cur][0].data_ptr())):
+                if self._clock_next != self.step_count + 1:
+                    self.clock[(self.step_count + 1) & 1].fill_(self.step_count + 1)
+                g.replay()
+                self.step_count += self.graph_steps
+                self._clock_next = self.step_count + 1
+                n -= self.graph_steps
+            else:
                 self.step_count += 1
                 self.launch_step(self.step_count)
+                n -= 1
+
+    def step(self, n: int = 1, check: bool = True, check_every: int = 200) -> None:
+        """Advance n steps (replaying the graph of capture() where it fits).
+        With check=True the device error word is read every `check_every`
+        steps; a slot overflow rolls the state back to the start of that
+        chunk, widens the slot template (4 -> 8 -> 16) and redoes the chunk,
+        so no phase is ever dropped silently."""
+        n = int(n)
+        if not check:
+            self._advance(n)
             return
         done = 0
         while done < n:
             chunk = min(int(check_every), n - done)
             ckpt = [t.clone() for t in self.buf[self.cur]], self.step_count
-            for _ in range(chunk):
-                self.step_count += 1
-                self.launch_step(self.step_count)
+            self._advance(chunk)
             v = int(self.err.item())
             if v & 8 and self.slots < max(_SLOT_TEMPLATES):
                 self.err.zero_()
@@ -260,6 +315,7 @@ class CompactSolver:
         i2[: old * self.cells].copy_(idx)
         v2[: old * self.cells].copy_(val)
         self.step_count = steps
+        self.graph = None  # captured for the old buffers
         self.forget_history()
 
     def autotune(self, steps: int = 8, use_cache: bool = True) -> dict:

@@ -232,6 +232,51 @@ def test_two_stream_step_replays_from_a_cuda_graph():
     b.check()
 
 
+def test_device_clock_equals_temperature_by_value():
+    """mpf3d_compact_step_clocked (temperature from the device step clock)
+    gives the state of mpf3d_compact_step_tuned with T_melt + s * rate passed
+    by value, bit for bit, under fast cooling."""
+    import ctypes
+    from mpf3d import _lib, inputs
+    case = inputs.voronoi_case(32, 24, 32, 8, 10, seed=5, orientation_seed=2, undercooling=1.0)
+    a, b = make_solver(case, cooling_rate=0.37), make_solver(case, cooling_rate=0.37)
+    a.step(7, check=False)  # the solver's own stepping: the clocked entry
+    for s in range(1, 8):
+        src, dst = b.buf[b.cur], b.buf[1 - b.cur]
+        rc = _lib.lib().mpf3d_compact_step_tuned(
+            src[0].data_ptr(), src[1].data_ptr(), src[2].data_ptr(), dst[0].data_ptr(), dst[1].data_ptr(),
+            dst[2].data_ptr(), b.slots, b.amax, b.T0z.data_ptr(), b.T_melt + s * b.cooling_rate,
+            b.wij.data_ptr(), b.a2ij.data_ptr(), b.mij.data_ptr(), b.n111.data_ptr(), b.N, b.nx, b.ny, b.nz,
+            ctypes.byref(b.scalars), 1, 1, int(b.symmetric_normals), b.work_items.data_ptr(),
+            b.work_count.data_ptr(), s & 1, b.err.data_ptr(), b._stream(), None, b.tile_flags.data_ptr(),
+            _lib.STEP_MULTI_LIST)
+        _lib.check(rc, "compact_step_tuned")
+        b.cur = 1 - b.cur
+    assert np.array_equal(a.to_dense(), b.to_dense())
+    a.check()
+    b.check()
+
+
+def test_captured_steps_replay_repeatedly_and_keep_cooling():
+    """capture(4) then step(13): three graph replays and one eager step, with
+    eager steps before; the temperature keeps falling across replays (the
+    device clock), so the state equals 14 eager steps bit for bit.  With fast
+    cooling a replay that repeated the captured temperatures would differ."""
+    from mpf3d import inputs
+    case = inputs.voronoi_case(32, 24, 32, 8, 10, seed=5, orientation_seed=2, undercooling=1.0)
+    a, b = make_solver(case, cooling_rate=0.37), make_solver(case, cooling_rate=0.37)
+    a.sweep_tma = b.sweep_tma = True
+    a.step(14, check=False)
+    b.step(1, check=False)
+    b.capture(4)
+    b.step(13)
+    torch.cuda.synchronize()
+    assert b.step_count == 14
+    assert np.array_equal(a.to_dense(), b.to_dense())
+    a.check()
+    b.check()
+
+
 def test_pinned_host_conversion_in_place():
     """Dense phi in pinned host memory is converted in place over the CPU-GPU
     link (no device copy) and written back in place: the state and the
