@@ -543,6 +543,10 @@ __device__ __forceinline__ void update_cell(const In &in, const Out &out, const 
     const double Tmc = P.clock ? P.clock->tmc[P.parity] : P.Tmc;
     const float dT = P.t_uniform ? P.dT_uniform : (float)(M.T0z[k] - Tmc);
     const float inv_n = 1.0f / (float)(n > 0 ? n : 1);
+    // the non-heavy build: lap_sl is eps0^2 times the liquid's Laplacian for
+    // every solid (the isotropic branch above) and b_sl is 1, so its arrays
+    // stay out of local memory
+    const float lsl_iso = (has_liq && has_solid) ? P.eps0sq * lap[0] : 0.0f;
     float outv[NA];
 #pragma unroll 1
     for (int t1 = 0; t1 < nn; ++t1) {
@@ -553,13 +557,16 @@ __device__ __forceinline__ void update_cell(const In &in, const Out &out, const 
             if (t2 == t1) continue;
             const int j = ids[t2];
             const bool sl = (i != LIQ && j == LIQ), ls = (i == LIQ && j != LIQ);
-            const float T = sl ? 0.5f * lap_sl[t1] : (ls ? -0.5f * lap_sl[t2] : 0.5f * __fsub_rn(Ag[t1], Ag[t2]));
+            const float L1 = HEAVY ? lap_sl[t1] : lsl_iso, L2 = HEAVY ? lap_sl[t2] : lsl_iso;
+            const float T = sl ? 0.5f * L1 : (ls ? -0.5f * L2 : 0.5f * __fsub_rn(Ag[t1], Ag[t2]));
             const float ppp = __fadd_rn(__fsub_rn(W[t1], W[t2]), T);
             const float df = sl ? -P.Sf * dT : (ls ? P.Sf * dT : 0.0f);
             const float tf = __fmul_rn(__fmul_rn(FORCE_PREF, sqrtf(fmaxf(__fmul_rn(vc[t1], vc[t2]), 0.0f))), df);
             float me = __ldg(M.mij + i * N + j);
-            if (sl) me *= b_sl[t1];
-            else if (ls) me *= b_sl[t2];
+            if (HEAVY) {
+                if (sl) me *= b_sl[t1];
+                else if (ls) me *= b_sl[t2];
+            }
             dpi = __fsub_rn(dpi, __fmul_rn(__fmul_rn(__fmul_rn(2.0f, me), inv_n), __fsub_rn(ppp, tf)));
         }
         outv[t1] = fminf(fmaxf(fmaf(P.dt, dpi, vc[t1]), 0.0f), 1.0f);
