@@ -122,6 +122,13 @@ def test_slot_template_widens_instead_of_dropping_phases():
     b = make_solver(case, slots=16)
     b.step(6)
     assert np.array_equal(a.to_dense(), b.to_dense())
+    # the same with the steps replayed from a captured graph: the overflow
+    # rolls back to eager steps on the widened buffers
+    c = make_solver(case, slots=4)
+    c.capture(2)
+    c.step(6, check_every=2)
+    assert c.slots > 4 and c.graph is None
+    assert np.array_equal(c.to_dense(), b.to_dense())
 
 
 def test_owner_map_start_equals_dense_start():
