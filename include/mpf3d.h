@@ -168,22 +168,22 @@ int mpf3d_compact_active_count(const uint32_t *head, const uint16_t *idx, int sl
  * zeroed once before the first step; `parity` alternates 0/1 on consecutive
  * steps so no reset is needed in between.  Cells must number fewer than 2^31.
  * Streams: with anisotropy on, the interface kernel runs on a library-owned
- * second stream of the device, beside the general kernel, forked from and
- * joined back to `stream` by events; to the caller the step is ordered on
- * `stream` like one kernel.  The second stream is created by the first such
- * call made outside a stream capture; a call inside a capture before that
- * launches both kernels on `stream`.  The same holds for
- * mpf3d_compact_step_tuned and mpf3d_compact_step_noalloc; the batched step
- * (mpf3d_batched_step) runs on `stream` alone.  The second stream is shared
- * by the device's callers: while a capture that holds a step is open, run no
- * uncaptured step of that device from another host thread.  Because every
- * caller's interface kernel goes through that one stream, steps of several
- * solvers issued on independent streams of one device are serialised with
- * each other. */
-/* Creates the current device's second stream (see "Streams" below) now, so
- * that steps captured into a CUDA graph later run their general and
- * interface kernels side by side.  Fails (MPF3D_ERR_CUDA) when `stream` is
- * being captured.  Optional: the first uncaptured step does the same. */
+ * second stream, beside the general kernel, forked from and joined back to
+ * `stream` by events; to the caller the step is ordered on `stream` like one
+ * kernel.  Each caller stream of each device gets its own second stream and
+ * event pair, created by its first such call made outside a stream capture;
+ * a call inside a capture before that launches both kernels on `stream`.
+ * Steps that callers issue on independent streams therefore stay
+ * independent.  The same holds for mpf3d_compact_step_tuned,
+ * mpf3d_compact_step_clocked and mpf3d_compact_step_noalloc; the batched step
+ * (mpf3d_batched_step) runs on `stream` alone.  The second streams and events
+ * live until the process ends; cudaDeviceReset is not supported after a
+ * step. */
+/* Creates the second stream of `stream` on the current device (see
+ * "Streams" above) now, so that steps captured from `stream` into a CUDA
+ * graph later run their general and interface kernels side by side.  Fails
+ * (MPF3D_ERR_CUDA) when `stream` is being captured.  Optional: the first
+ * uncaptured step on `stream` does the same. */
 int mpf3d_streams_prepare(void *stream);
 
 int mpf3d_compact_step(const uint32_t *head, const uint16_t *idx, const float *val, uint32_t *head_out,

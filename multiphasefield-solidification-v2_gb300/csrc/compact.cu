@@ -32,6 +32,7 @@
 #include <string.h>
 
 #include <mutex>
+#include <unordered_map>
 
 #include "compact_state.cuh"
 #include "mpf3d.h"
@@ -1456,15 +1457,22 @@ dim3 zfast_grid(int nx, int ny, int nz, dim3 b) {
 // fills each other's idle issue slots.  Created on first use outside a
 // stream capture; the fork/join is enqueued under the mutex so that callers
 // on other host threads cannot interleave their event records with it.
+// The second stream of a step and its fork/join events, one set per
+// (device, caller stream): steps that callers issue on independent streams
+// stay independent of each other.
 struct SideStream {
-    std::mutex mu;
     bool ready = false;
     cudaStream_t stream = nullptr;
     cudaEvent_t fork = nullptr, join = nullptr;
 };
 
-SideStream &side_stream_of(int dev) {
-    static SideStream all[64];
+struct SideTable {
+    std::mutex mu;
+    std::unordered_map<cudaStream_t, SideStream> by_caller;  // element references survive rehashing
+};
+
+SideTable &side_table_of(int dev) {
+    static SideTable all[64];
     return all[dev & 63];
 }
 
@@ -1482,7 +1490,7 @@ bool side_ready(SideStream &side, cudaStream_t s) {
 }
 
 // general(stream) and interface(stream) launch the two work-list kernels of
-// a step; with `both`, the interface kernel goes to the device's side stream,
+// a step; with `both`, the interface kernel goes to the caller stream's side stream,
 // forked from s after the sweep and joined back before s continues.
 template <class General, class Interface>
 void launch_side_by_side(cudaStream_t s, bool both, General &&general, Interface &&interface) {
@@ -1492,8 +1500,9 @@ void launch_side_by_side(cudaStream_t s, bool both, General &&general, Interface
     }
     int dev = 0;
     cudaGetDevice(&dev);
-    SideStream &side = side_stream_of(dev);
-    std::lock_guard<std::mutex> lock(side.mu);
+    SideTable &tab = side_table_of(dev);
+    std::lock_guard<std::mutex> lock(tab.mu);
+    SideStream &side = tab.by_caller[s];
     if (!side_ready(side, s)) {  // first call inside a capture: both kernels on the caller's stream
         general(s);
         interface(s);
@@ -1731,9 +1740,9 @@ const mpf3d_tuning kBatchedDefault = {4, 8, 8, 256, 8, 128};
 extern "C" int mpf3d_streams_prepare(void *stream) {
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return MPF3D_ERR_CUDA;
-    SideStream &side = side_stream_of(dev);
-    std::lock_guard<std::mutex> lock(side.mu);
-    return side_ready(side, (cudaStream_t)stream) ? MPF3D_OK : MPF3D_ERR_CUDA;
+    SideTable &tab = side_table_of(dev);
+    std::lock_guard<std::mutex> lock(tab.mu);
+    return side_ready(tab.by_caller[(cudaStream_t)stream], (cudaStream_t)stream) ? MPF3D_OK : MPF3D_ERR_CUDA;
 }
 
 // The body of mpf3d_compact_step_tuned and mpf3d_compact_step_clocked

@@ -239,6 +239,31 @@ def test_two_stream_step_replays_from_a_cuda_graph():
     b.check()
 
 
+def test_solvers_on_independent_streams():
+    """Two solvers stepped on two streams (each with its own second stream
+    for the interface kernel), interleaved from the host, give the state of
+    a solver stepped alone, bit for bit."""
+    from mpf3d import inputs
+    case = inputs.voronoi_case(32, 24, 32, 8, 10, seed=5, orientation_seed=2, undercooling=2.0)
+    ref, a, b = make_solver(case), make_solver(case), make_solver(case)
+    ref.step(6, check=False)
+    dev = torch.device("cuda:0")
+    s1, s2 = torch.cuda.Stream(dev), torch.cuda.Stream(dev)
+    s1.wait_stream(torch.cuda.current_stream(dev))
+    s2.wait_stream(torch.cuda.current_stream(dev))
+    for _ in range(6):
+        with torch.cuda.stream(s1):
+            a.step(1, check=False)
+        with torch.cuda.stream(s2):
+            b.step(1, check=False)
+    torch.cuda.synchronize()
+    want = ref.to_dense()
+    assert np.array_equal(a.to_dense(), want)
+    assert np.array_equal(b.to_dense(), want)
+    for s in (ref, a, b):
+        s.check()
+
+
 def test_device_clock_equals_temperature_by_value():
     """mpf3d_compact_step_clocked (temperature from the device step clock)
     gives the state of mpf3d_compact_step_tuned with T_melt + s * rate passed
