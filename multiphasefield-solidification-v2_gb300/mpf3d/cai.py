@@ -54,10 +54,13 @@ def stream_handle(cfg_stream, arrays) -> int:
     """Stream to enqueue on: the launch-config stream if given, else the CAI
     stream of the first array that names one, else the legacy default stream."""
     if cfg_stream is not None and cfg_stream != 0:
-        h = getattr(cfg_stream, "handle", cfg_stream)
-        h = getattr(h, "value", h)
-        if hasattr(cfg_stream, "cuda_stream"):
+        if hasattr(cfg_stream, "cuda_stream"):  # torch
             h = cfg_stream.cuda_stream
+        elif hasattr(cfg_stream, "ptr"):  # CuPy
+            h = cfg_stream.ptr
+        else:  # Numba (handle is a ctypes pointer) or a raw handle
+            h = getattr(cfg_stream, "handle", cfg_stream)
+            h = getattr(h, "value", h)
         return int(h or 0)
     for a in arrays:
         s = a.stream
