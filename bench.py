@@ -875,6 +875,7 @@ def run_c3(args):
     s = CompactSolver.from_owner(owner, prof, temp, n111, wij, aij, mij, phys, slots=args.slots)
     setup = time.perf_counter() - t0
     s.step(args.warmup)
+    tuned = s.autotune(steps=4) if not args.no_autotune else None  # trials restore the state
     torch.cuda.synchronize(dev)
     stream = torch.cuda.current_stream(dev)
     e0 = torch.cuda.Event(enable_timing=True)
@@ -897,7 +898,10 @@ def run_c3(args):
                                    "anisotropy+torque, uniform cooling, FP32 compact, started from the owner map",
                        "slots": s.slots, "state_bytes_per_buffer": s.state_bytes()},
             "setup_s": setup, "stored_phases_per_cell_end": float(s.stored_counts().double().mean().item()),
-            "clocks": clk.summary(), "gpu_launches": 3 * args.steps}
+            "clocks": clk.summary(), "gpu_launches": 3 * args.steps,
+            "launch_shape": {"config": list(tuned["config"]), "sweep_tma": bool(s.sweep_tma),
+                             "ms_per_step_tuned": tuned["ms_per_step"],
+                             "ms_per_step_default": tuned["default_ms_per_step"]} if tuned else None}
     print(json.dumps(line), flush=True)
 
 
